@@ -1,0 +1,167 @@
+/*
+ * bm4dof.h -- C ABI of the GB300 (sm_103a) BM4D-OF / NL-DCT video denoising path.
+ *
+ * The entry points mirror the reference's C++ interface in namespace VideoNLB
+ * (src/core/nldct.h).  Each declaration names the reference function it stands
+ * in for.  Plain pointers and sizes only: no C++ or torch types cross this
+ * boundary, so the library can be bound from C, ctypes or any FFI.
+ *
+ * Video layout (the reference's Video<float>, src/utils/lib_videot.hpp:88-92):
+ *   planar, value(x, y, t, c) = data[t*W*H*C + c*W*H + y*W + x].
+ * Optical flow uses the same layout with C = 2 (channel 0 = x displacement,
+ * channel 1 = y displacement).
+ *
+ * Errors: every call that can fail returns a bm4dof_status; the message of the
+ * last failure on the calling thread is available from bm4dof_last_error().
+ * The messages of the reference's std::runtime_error throws are kept verbatim
+ * (src/core/nldct.cpp:279,289,296,334,341,634).
+ */
+#ifndef BM4DOF_H_INCLUDED
+#define BM4DOF_H_INCLUDED
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bm4dof_status {
+	BM4DOF_OK = 0,
+	BM4DOF_ERR_ARGUMENT = 1,      /* null pointer, zero size, bad flag            */
+	BM4DOF_ERR_CHANNELS = 2,      /* nldct.cpp:279  channels not 1, 3 or 4         */
+	BM4DOF_ERR_FWD_FLOW = 3,      /* nldct.cpp:289  forward flow size mismatch     */
+	BM4DOF_ERR_BWD_FLOW = 4,      /* nldct.cpp:296  backward flow size mismatch    */
+	BM4DOF_ERR_NO_STEP = 5,       /* nldct.cpp:334  both patch sizes are zero      */
+	BM4DOF_ERR_BASIC_SIZE = 6,    /* nldct.cpp:341  basic size differs from noisy  */
+	BM4DOF_ERR_BIOR_SIZE = 7,     /* nldct.cpp:634  bior1.5 with patch size != 8   */
+	BM4DOF_ERR_UNSUPPORTED = 8,   /* parameter combination this build rejects      */
+	BM4DOF_ERR_CUDA = 9,          /* CUDA runtime error (message has the details)  */
+	BM4DOF_ERR_NO_MEMORY = 10,    /* device or host allocation failed              */
+	BM4DOF_ERR_TIMEOUT = 11,      /* a bounded device-side wait ran out            */
+	BM4DOF_ERR_NO_DEVICE = 12     /* no usable CUDA device                          */
+} bm4dof_status;
+
+typedef enum bm4dof_color_space { BM4DOF_RGB = 0, BM4DOF_YUV = 1 } bm4dof_color_space;
+typedef enum bm4dof_transform  { BM4DOF_DCT = 0, BM4DOF_BIOR1_5 = 1 } bm4dof_transform;
+
+/* Mirror of VideoNLB::nlbParams (src/core/nldct.h:55-82), field for field. */
+typedef struct bm4dof_params {
+	float    sigma;
+	unsigned sizePatch;
+	unsigned sizePatchTime;
+	unsigned nSimilarPatches;
+	unsigned sizeSearchWindow;
+	unsigned sizeSearchTimeRangeFwd;
+	unsigned sizeSearchTimeRangeBwd;
+	unsigned boundary;
+	unsigned offSet;
+	unsigned offSetTime;
+	float    beta;
+	float    betaMean;
+	float    tau;
+	int      orderInvariance;
+	int      isFirstStep;
+	int      doPasteBoost;
+	int      verbose;
+	int      colorSpace;            /* bm4dof_color_space */
+	int      transform;             /* bm4dof_transform   */
+	unsigned sizeSearchWindowPred;
+	unsigned nSimilarPatchesPred;
+	float    dsub;
+	int      agg_window;
+} bm4dof_params;
+
+/* Mirror of VideoSize (src/utils/lib_videot.hpp:40-51): the four sizes. */
+typedef struct bm4dof_video_size {
+	unsigned width;
+	unsigned height;
+	unsigned frames;
+	unsigned channels;
+} bm4dof_video_size;
+
+/* ---- parameter resolution (host only, no device needed) ------------------ */
+
+/* VideoNLB::initializeNlbParameters, src/core/nldct.cpp:81-148.
+ * betaMean is set to beta here; the reference leaves it uninitialised unless
+ * -b1/-bm1 is given (it is read only by the order-invariant filter). */
+void bm4dof_initialize_params(bm4dof_params *params, unsigned step, float sigma,
+                              const bm4dof_video_size *size, int verbose);
+
+/* VideoNLB::setSizeSearchWindow, src/core/nldct.cpp:160-168. */
+void bm4dof_set_size_search_window(bm4dof_params *params, unsigned sizeSearchWindow);
+
+/* VideoNLB::setSizePatch, src/core/nldct.cpp:179-188. */
+void bm4dof_set_size_patch(bm4dof_params *params, const bm4dof_video_size *size,
+                           unsigned sizePatch);
+
+/* VideoNLB::setNSimilarPatches, src/core/nldct.cpp:199-210. */
+void bm4dof_set_n_similar_patches(bm4dof_params *params, unsigned nSimilarPatches);
+
+/* VideoNLB::printNlbParameters, src/core/nldct.cpp:219-249: writes the same
+ * text into buf (NUL-terminated, truncated to len) and returns its length. */
+int bm4dof_format_params(const bm4dof_params *params, char *buf, size_t len);
+
+/* VideoNLB::printNlbParameters to stdout. */
+void bm4dof_print_params(const bm4dof_params *params);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *bm4dof_last_error(void);
+
+/* Library version string. */
+const char *bm4dof_version(void);
+
+/* ---- device context ------------------------------------------------------ */
+
+typedef struct bm4dof_ctx bm4dof_ctx;
+
+/* Creates a context bound to one CUDA device with its own stream.  Calls on one
+ * context are serialised; distinct contexts may run concurrently. */
+bm4dof_status bm4dof_create(bm4dof_ctx **ctx, int device);
+void          bm4dof_destroy(bm4dof_ctx *ctx);
+
+/* Flags for bm4dof_run. */
+#define BM4DOF_DEVICE_POINTERS  0x1u  /* all video pointers are device pointers  */
+#define BM4DOF_KEEP_GROUPS      0x2u  /* record neighbour lists for inspection   */
+#define BM4DOF_MIXED_PRECISION  0x4u  /* FP16 distance pre-screen + BF16 transforms */
+
+/* VideoNLB::runNlBayes, src/core/nldct.cpp:267-478.
+ *
+ *  noisy        W*H*C*F floats.
+ *  fflow,bflow  W*H*2*F floats each, or both NULL for no flow (the reference's
+ *               empty Video, nldct.cpp:283).
+ *  basic        W*H*C*F floats: output of step 1, or input when
+ *               params1->sizePatch == 0 (step 2 only, nldct.cpp:329-342).
+ *  final        W*H*C*F floats: output of step 2 (untouched when
+ *               params2->sizePatch == 0).
+ *  nparts       number of spatial tiles; the reference uses
+ *               2*omp_get_max_threads() (nldct.cpp:318-323).  0 means 2.
+ *  ratios       out: percentage of processed groups per step (the reference's
+ *               return value).  May be NULL.
+ */
+bm4dof_status bm4dof_run(bm4dof_ctx *ctx,
+                         const float *noisy, const float *fflow, const float *bflow,
+                         unsigned width, unsigned height, unsigned channels, unsigned frames,
+                         float *basic, float *final_,
+                         const bm4dof_params *params1, const bm4dof_params *params2,
+                         unsigned nparts, unsigned flags, float ratios[2]);
+
+/* Neighbour lists of the last bm4dof_run made with BM4DOF_KEEP_GROUPS, for one
+ * step (1 or 2) and tile.  For each processed group in processing order:
+ *   ref[g]          reference patch index (tile video index at channel 0, as
+ *                   the reference's ij3 = sz.index(px,py,pt,0), nldct.cpp:765),
+ *   nsimp[g]        number of similar patches kept (nldct.cpp:1284-1289),
+ *   index[g*stride + n]  the reference's index[n] (nldct.cpp:1300-1301).
+ * Writes at most cap groups and returns the total count in *count. */
+bm4dof_status bm4dof_get_groups(bm4dof_ctx *ctx, unsigned step, unsigned tile,
+                                unsigned *ref, unsigned *nsimp, unsigned *index,
+                                unsigned stride, size_t cap, size_t *count);
+
+/* Per-stage device times (milliseconds) of the last bm4dof_run: search,
+ * filter, aggregation, other; and the number of kernel launches it made. */
+bm4dof_status bm4dof_last_timings(bm4dof_ctx *ctx, float ms[4], unsigned *launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BM4DOF_H_INCLUDED */
