@@ -156,9 +156,11 @@ bm4dof_status bm4dof_get_groups(bm4dof_ctx *ctx, unsigned step, unsigned tile,
                                 unsigned *ref, unsigned *nsimp, unsigned *index,
                                 unsigned stride, size_t cap, size_t *count);
 
-/* Per-stage device times (milliseconds) of the last bm4dof_run: search,
- * filter, aggregation, other; and the number of kernel launches it made. */
-bm4dof_status bm4dof_last_timings(bm4dof_ctx *ctx, float ms[4], unsigned *launches);
+/* Device times (milliseconds, CUDA events on the context's stream) of the
+ * last bm4dof_run: ms[0] patch search, ms[1] group filter, ms[2] aggregation,
+ * ms[3] everything else (copies, colour, normalisation), ms[4] the whole call
+ * from its first to its last event; and the number of kernel launches. */
+bm4dof_status bm4dof_last_timings(bm4dof_ctx *ctx, float ms[5], unsigned *launches);
 
 #ifdef __cplusplus
 }

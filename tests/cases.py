@@ -1,0 +1,18 @@
+"""Seeded parity workloads shared by the oracle, golden and GPU tests.
+Each case: (name, W, H, F, C, sigma, seed, flow, cli-params, nthreads)."""
+CFG_VIDEO = dict(px1=4, px2=4, pt1=4, pt2=4, wx1=21, wx2=21, np1=16, np2=16, b1=3.0)
+CFG_IMAGE = dict(px1=8, px2=8, pt1=1, pt2=1, wx1=21, wx2=21, np1=16, np2=16, b1=3.0)
+
+CASES = [
+    ("image_px8", 48, 40, 1, 1, 20.0, 11, False, CFG_IMAGE, 1),
+    ("image_defaults", 40, 36, 1, 1, 20.0, 12, False, {}, 1),
+    ("image_sigma45", 40, 36, 1, 1, 45.0, 17, False, dict(px2=7), 1),
+    ("video_px4", 40, 36, 6, 1, 20.0, 13, True, CFG_VIDEO, 1),
+    ("video_px4_4tiles", 44, 40, 6, 1, 20.0, 14, True, CFG_VIDEO, 2),
+    ("video_noflow", 36, 32, 5, 1, 20.0, 15, False, CFG_VIDEO, 1),
+    ("video_6tiles", 52, 34, 5, 1, 10.0, 18, True, CFG_VIDEO, 3),
+    ("video_misc", 40, 36, 5, 1, 30.0, 16, True,
+     dict(px1=8, px2=7, pt1=1, pt2=1, wx1=9, wx2=11, np1=8, np2=32), 1),
+    ("rgb_image", 40, 36, 1, 3, 20.0, 19, False, CFG_IMAGE, 1),
+    ("rgb_video", 30, 28, 4, 3, 20.0, 20, True, CFG_VIDEO, 1),
+]

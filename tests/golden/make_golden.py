@@ -1,0 +1,40 @@
+"""Generate tests/golden/*.npz by running the reference's own code (built
+from its sources into oracle/_ref by oracle/Makefile) on the seeded cases of
+tests/cases.py.  Inputs are stored with the outputs, so the fixtures do not
+depend on the random generator of the machine that reads them.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+from helpers import resolve_params, video_case  # noqa: E402
+from cases import CASES  # noqa: E402
+import pyoracle  # noqa: E402
+
+FIELDS = [f for f, _ in pyoracle.Params._fields_]
+
+
+def main():
+    pyoracle.build()
+    ref = pyoracle.Reference()
+    for (name, W, H, F, C, sigma, seed, flow, cli, nthreads) in CASES:
+        clean, nz, ff, bf = video_case(W, H, F, sigma=sigma, seed=seed, channels=C, flow=flow)
+        p1, p2 = resolve_params(ref, (W, H, F, C), sigma, **cli)
+        basic, final, ratios = ref.runNlBayes(nz, ff, bf, p1, p2, nthreads=nthreads)
+        out = dict(noisy=nz, clean=clean, basic=basic, final=final, ratios=np.array(ratios, np.float32),
+                   nthreads=np.array(nthreads), sigma=np.array(sigma, np.float32))
+        if ff is not None:
+            out["fflow"], out["bflow"] = ff, bf
+        for tag, p in (("p1", p1), ("p2", p2)):
+            out[tag] = np.array([float(getattr(p, f)) for f in FIELDS], np.float64)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, ratios)
+
+
+if __name__ == "__main__":
+    main()
