@@ -143,9 +143,11 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
 	const int spc = sp.spc, C = sp.C, np = sp.np;
 	const int nsp = nsp_of(np);
 	const int tile_f = C * spc * nsp;          // floats of one group tile (all channels)
+	const int bsz = ((spc * spc + 3) / 4) * 4; // basis sizes padded: the group tiles
+	                                           // below must start on 16-byte boundaries
 	float *Bt = sm;                            // Bt[p*spc + k] = basis[k*spc + p]
-	float *Bi = Bt + spc * spc;                // Bi[k*spc + p] = binv[k*spc + p]
-	float *wn = Bi + spc * spc;                // window
+	float *Bi = Bt + bsz;                      // Bi[k*spc + p] = binv[k*spc + p]
+	float *wn = Bi + bsz;                      // window
 	float *Gn = wn + ((spc + 3) / 4) * 4;      // noisy group   [c][p][n]
 	float *Zn = Gn + tile_f;                   // its transform [c][k][n]
 	float *Gb = Zn + tile_f;                   // basic group (step 2); later Wiener w^2
@@ -313,7 +315,8 @@ size_t filter_smem_bytes(const StepParams &sp)
 {
 	const int nsp = ((sp.np + 3) / 4) * 4 + 4;
 	const size_t tile_f = (size_t)sp.C * sp.spc * nsp;
-	return sizeof(float) * (2 * (size_t)sp.spc * sp.spc + ((sp.spc + 3) / 4) * 4 + 4 * tile_f);
+	const size_t bsz = ((size_t)sp.spc * sp.spc + 3) / 4 * 4;
+	return sizeof(float) * (2 * bsz + ((sp.spc + 3) / 4) * 4 + 4 * tile_f);
 }
 
 cudaError_t launch_filter(const Image &noisy, const Image &basic, const Tile *tiles, int ntiles,
