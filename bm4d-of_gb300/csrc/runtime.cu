@@ -219,7 +219,7 @@ Image image(float *p, unsigned W, unsigned H, unsigned C, unsigned F)
 	return im;
 }
 
-bm4dof_status check_params(const bm4dof_params &p, unsigned W, unsigned H, unsigned C, unsigned F)
+bm4dof_status check_params(const bm4dof_params &p)
 {
 	if (p.transform == BM4DOF_BIOR1_5 && p.sizePatch != 8) {
 		set_error("VideoNLB::processNlBayes: bior1_5 transform is only implemented for patches of size 8 x 8 x pt.");
@@ -227,8 +227,7 @@ bm4dof_status check_params(const bm4dof_params &p, unsigned W, unsigned H, unsig
 	}
 	const unsigned spc = p.sizePatch * p.sizePatch * p.sizePatchTime;
 	std::string why;
-	if (p.sizePatchTime == 0 || p.sizePatchTime > F) why = "sizePatchTime must be in [1, frames]";
-	else if (p.sizePatch > W || p.sizePatch > H) why = "sizePatch larger than the video";
+	if (p.sizePatchTime == 0 || p.sizePatch == 0) why = "patch sizes must be positive";
 	else if (p.offSet == 0 || p.offSetTime == 0) why = "offSet and offSetTime must be positive";
 	else if (p.nSimilarPatches == 0 || p.nSimilarPatches > (unsigned)kMaxNp) why = "nSimilarPatches must be in [1, 32]";
 	else if (spc > (unsigned)kMaxSpc) why = "sizePatch^2 * sizePatchTime must be at most 64";
@@ -545,7 +544,7 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
 	for (int s = 1; s <= 2; s++) {
 		if (s == 1 && step == 2) continue;
 		if (s == 2 && step == 1) continue;
-		bm4dof_status e = check_params(s == 1 ? *p1 : *p2, W, H, C, F);
+		bm4dof_status e = check_params(s == 1 ? *p1 : *p2);
 		if (e != BM4DOF_OK) return e;
 	}
 	CK(cudaSetDevice(ctx->device));

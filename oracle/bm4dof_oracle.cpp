@@ -941,8 +941,7 @@ int oracle_run(const float *noisy_in, const float *fflow_in, const float *bflow_
 		if (!p->sizePatch) continue;
 		if (p->transform == BM4DOF_BIOR1_5 && p->sizePatch != 8)
 			return fail(err, errlen, "VideoNLB::processNlBayes: bior1_5 transform is only implemented for patches of size 8 x 8 x pt.", BM4DOF_ERR_BIOR_SIZE);
-		if (p->offSet == 0 || p->offSetTime == 0 || p->sizePatchTime == 0 || p->sizePatchTime > F ||
-		    p->sizePatch > W || p->sizePatch > H)
+		if (p->offSet == 0 || p->offSetTime == 0 || p->sizePatchTime == 0)
 			return fail(err, errlen, "oracle: unsupported parameters", BM4DOF_ERR_UNSUPPORTED);
 		if (p->doPasteBoost)
 			return fail(err, errlen, "oracle: doPasteBoost is not restated", BM4DOF_ERR_UNSUPPORTED);

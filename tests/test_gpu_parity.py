@@ -88,7 +88,24 @@ def test_gpu_constant_video_stale_weights(gpulib, gpuctx, oracle):
     pg = resolve_params(gpulib, (W, H, F, 1), 20.0, **CFG_VIDEO)
     ob, of, orat = oracle.runNlBayes(nz, None, None, *po, nparts=2)
     gb, gf, grat = gpuctx.runNlBayes(nz, None, None, *pg, nparts=2)
-    assert np.array_equal(gb, ob) and np.array_equal(gf, of) and grat == orat
+    # this degenerate input makes the reference itself produce NaNs (zero
+    # Wiener energy): they must appear at the same pixels
+    assert np.isnan(of).any()
+    assert np.array_equal(gb, ob, equal_nan=True) and np.array_equal(gf, of, equal_nan=True)
+    assert grat == orat
+
+
+def test_gpu_patch_longer_than_video(gpulib, gpuctx, oracle):
+    # pt > frames: no reference patch fits, every pixel takes 0 / noisy
+    # (nldct.cpp:537, 2446)
+    W, H, F = 24, 20, 3
+    clean, nz, ff, bf = video_case(W, H, F, seed=9)
+    po = resolve_params(oracle, (W, H, F, 1), 20.0, **CFG_VIDEO)
+    pg = resolve_params(gpulib, (W, H, F, 1), 20.0, **CFG_VIDEO)
+    ob, of, orat = oracle.runNlBayes(nz, ff, bf, *po, nparts=2)
+    gb, gf, grat = gpuctx.runNlBayes(nz, ff, bf, *pg, nparts=2)
+    assert grat == orat == (0.0, 0.0)
+    assert np.array_equal(gb, ob, equal_nan=True) and np.array_equal(gf, of, equal_nan=True)
 
 
 def test_gpu_step2_only_and_step1_only(gpulib, gpuctx, oracle):
@@ -137,7 +154,12 @@ def test_gpu_errors(gpulib, gpuctx):
     with pytest.raises(gpulib.BM4DOFError) as e:
         gpuctx.runNlBayes(nz, None, None, *q)
     assert e.value.status == "ERR_BIOR_SIZE"
+    q = resolve_params(gpulib, (W, H, F, 1), 20.0, **CFG_VIDEO)
+    q[1].nSimilarPatches = 64
+    with pytest.raises(gpulib.BM4DOFError) as e:
+        gpuctx.runNlBayes(nz, None, None, *q)
+    assert e.value.status == "ERR_UNSUPPORTED"
     # the context stays usable after errors
-    clean, nz, ff, bf = video_case(W + 8, H + 8, F, seed=3)
-    p = resolve_params(gpulib, (W + 8, H + 8, F, 1), 20.0, **CFG_VIDEO)
+    clean, nz, ff, bf = video_case(W + 8, H + 8, F + 3, seed=3)
+    p = resolve_params(gpulib, (W + 8, H + 8, F + 3, 1), 20.0, **CFG_VIDEO)
     gpuctx.runNlBayes(nz, ff, bf, *p)
