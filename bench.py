@@ -43,6 +43,7 @@ WORKLOADS = {
     # name: (W, H, F, sigma, seed)
     "hd": (1920, 1080, 60, 20.0, 5),
     "c2": (854, 480, 20, 20.0, 2),
+    "small": (480, 272, 12, 20.0, 3),   # profiling case (about 1 GB on the device)
 }
 CLI = dict(px1=4, px2=4, pt1=4, pt2=4, wx1=21, wx2=21, np1=16, np2=16, b1=3.0)
 METRIC = "megapixel-frames/s at 1 GPU, plain vs learned/mixed at ≤0.05 dB PSNR loss"
