@@ -18,10 +18,6 @@ namespace bm4dof {
 
 namespace {
 
-constexpr int kGatherBX = 8, kGatherBY = 8;
-constexpr int kGatherThreads = kGatherBX * kGatherBY;
-constexpr int kRegionMax = 1024;      // origins feeding one 8x8 pixel block
-constexpr int kEntryCap = 4096;       // slots sorted in shared memory per block
 
 __device__ __forceinline__ void group_position(const Tile &T, const int *grid, long long g,
                                                int &x, int &y, int &t)
@@ -191,122 +187,147 @@ __global__ void scan_add_kernel(unsigned *__restrict__ data, size_t n, const uns
 }
 
 // ---------------------------------------------------------------------------
-// ordered gather into one tile's sums (one 8x8 pixel block of one frame)
+// spatial lists: for every tile position (x, y, t'), the slots whose origin
+// lies in frame t' and whose patch covers (x, y), merged into slot order.
+// Entry = slot << 6 | dy << 3 | dx (dx, dy < 8 since px <= 8).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kGatherThreads)
-gather_kernel(Tile T, StepParams sp, int f_lo, const unsigned *__restrict__ off,
-              const unsigned *__restrict__ list, const float *__restrict__ vals,
-              const float *__restrict__ wslot, const float *__restrict__ win,
-              float *__restrict__ acc, float *__restrict__ wacc)
+__global__ void slist_count_kernel(int w, int h, int F, int px, int pt, int t_lo, int t_hi,
+                                   const unsigned *__restrict__ off, unsigned *__restrict__ cnt)
 {
-	__shared__ unsigned s_start[kRegionMax], s_len[kRegionMax], s_pos[kRegionMax + 1];
-	__shared__ unsigned long long s_key[kEntryCap];
-	__shared__ float s_win[kMaxSpc];
-	const int px = sp.px, pt = sp.pt, spc = sp.spc, C = sp.C;
-	const int bx0 = blockIdx.x * kGatherBX, by0 = blockIdx.y * kGatherBY;
-	const int t = f_lo + blockIdx.z;
-	const int RX = kGatherBX + px - 1, RY = kGatherBY + px - 1, RT = pt;
-	const int NR = RX * RY * RT;
-	const int tid = threadIdx.x;
-	for (int i = tid; i < spc; i += blockDim.x) s_win[i] = win[i];
-
-	// lists of every origin that can cover the block: x in [bx0-px+1, bx0+8) ...
-	for (int r = tid; r < NR; r += blockDim.x) {
-		const int rx = r % RX, ry = (r / RX) % RY, rt = r / (RX * RY);
-		const int ox = bx0 - px + 1 + rx, oy = by0 - px + 1 + ry, ot = t - pt + 1 + rt;
-		unsigned st = 0, ln = 0;
-		if (ox >= 0 && oy >= 0 && ot >= 0 && ox <= T.w - px && oy <= T.h - px && ot <= sp.F - pt) {
-			const size_t lin = ((size_t)ot * T.h + oy) * T.w + ox;
-			st = off[lin];
-			ln = off[lin + 1] - st;
-		}
-		s_start[r] = st;
-		s_len[r] = ln;
-	}
-	__syncthreads();
-	if (tid == 0) {
-		unsigned run = 0;
-		for (int r = 0; r < NR; r++) { s_pos[r] = run; run += s_len[r]; }
-		s_pos[NR] = run;
-	}
-	__syncthreads();
-	const unsigned E = s_pos[NR];
-
-	const int lx = tid % kGatherBX, ly = tid / kGatherBX;
-	const int x = bx0 + lx, y = by0 + ly;
-	const bool inside = x < T.w && y < T.h;
-	float a[4] = {0.f, 0.f, 0.f, 0.f}, wa = 0.f;
-	size_t pix = 0;
-	if (inside) {
-		pix = ((size_t)t * T.h + y) * T.w + x;
-		wa = wacc[pix];
-		for (int c = 0; c < C; c++) a[c] = acc[(((size_t)t * C + c) * T.h + y) * T.w + x];
-	}
-
-	if (E <= (unsigned)kEntryCap) {
-		unsigned P2 = 1;
-		while (P2 < E) P2 <<= 1;
-		for (int r = tid; r < NR; r += blockDim.x)
-			for (unsigned j = 0; j < s_len[r]; j++)
-				s_key[s_pos[r] + j] = ((unsigned long long)list[s_start[r] + j] << 32) | (unsigned)r;
-		for (unsigned i = E + tid; i < P2; i += blockDim.x) s_key[i] = ~0ull;
-		__syncthreads();
-		// bitonic sort by slot number
-		for (unsigned k = 2; k <= P2; k <<= 1)
-			for (unsigned j = k >> 1; j > 0; j >>= 1) {
-				for (unsigned i = tid; i < P2; i += blockDim.x) {
-					const unsigned l = i ^ j;
-					if (l > i) {
-						const unsigned long long u = s_key[i], v = s_key[l];
-						const bool up = (i & k) == 0;
-						if ((u > v) == up) { s_key[i] = v; s_key[l] = u; }
-					}
+	const size_t npos = (size_t)w * h * F;
+	for (size_t pos = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pos < npos;
+	     pos += (size_t)gridDim.x * blockDim.x) {
+		const int x = (int)(pos % w), y = (int)((pos / w) % h), t = (int)(pos / ((size_t)w * h));
+		unsigned c = 0;
+		if (t >= t_lo && t <= t_hi && t <= F - pt)
+			for (int dy = 0; dy < px; dy++) {
+				const int oy = y - dy;
+				if (oy < 0 || oy > h - px) continue;
+				for (int dx = 0; dx < px; dx++) {
+					const int ox = x - dx;
+					if (ox < 0 || ox > w - px) continue;
+					const size_t o = ((size_t)t * h + oy) * w + ox;
+					c += off[o + 1] - off[o];
 				}
-				__syncthreads();
 			}
-		if (inside) {
-			for (unsigned e = 0; e < E; e++) {
-				const unsigned long long key = s_key[e];
-				const int r = (int)(key & 0xffffffffull);
-				const int rx = r % RX, ry = (r / RX) % RY, rt = r / (RX * RY);
-				const int dx = lx + px - 1 - rx, dy = ly + px - 1 - ry, dt = pt - 1 - rt;
-				if (dx < 0 || dx >= px || dy < 0 || dy >= px) continue;
-				const size_t slot = key >> 32;
-				const int p = (dt * px + dy) * px + dx;
-				const float *v = vals + slot * (size_t)(C * spc);
-				for (int c = 0; c < C; c++) a[c] = __fadd_rn(a[c], v[c * spc + p]);
-				wa = __fadd_rn(wa, __fmul_rn(wslot[slot], s_win[p]));
+		cnt[pos] = c;
+	}
+}
+
+// PX > 0: one list per patch offset (dy, dx), held in registers; PX == 0:
+// any patch size, lists compacted in local memory.
+template <int PX>
+__global__ void slist_build_kernel(int w, int h, int F, int px_rt, int pt, int t_lo, int t_hi,
+                                   const unsigned *__restrict__ off, const unsigned *__restrict__ list,
+                                   const unsigned *__restrict__ soff, unsigned *__restrict__ sl)
+{
+	constexpr int L = PX > 0 ? PX * PX : kMaxSpc;
+	const int px = PX > 0 ? PX : px_rt;
+	const size_t npos = (size_t)w * h * F;
+	for (size_t pos = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pos < npos;
+	     pos += (size_t)gridDim.x * blockDim.x) {
+		unsigned o = soff[pos];
+		if (soff[pos + 1] == o) continue;
+		const int x = (int)(pos % w), y = (int)((pos / w) % h), t = (int)(pos / ((size_t)w * h));
+		unsigned cur[L], end[L], head[L], tag[L];
+		int nl = 0;
+#pragma unroll
+		for (int l = 0; l < L; l++) head[l] = 0xffffffffu;
+#pragma unroll
+		for (int dy = 0; dy < (PX > 0 ? PX : 8); dy++) {
+			if (dy >= px) break;
+#pragma unroll
+			for (int dx = 0; dx < (PX > 0 ? PX : 8); dx++) {
+				if (dx >= px) break;
+				const int oy = y - dy, ox = x - dx;
+				unsigned a = 0, b = 0;
+				if (oy >= 0 && oy <= h - px && ox >= 0 && ox <= w - px) {
+					const size_t q = ((size_t)t * h + oy) * w + ox;
+					a = off[q];
+					b = off[q + 1];
+				}
+				const int l = PX > 0 ? dy * PX + dx : nl;
+				if (PX > 0 || a < b) {
+					cur[l] = a; end[l] = b; tag[l] = (unsigned)(dy << 3 | dx);
+					head[l] = a < b ? list[a] : 0xffffffffu;
+					nl++;
+				}
 			}
 		}
-	} else if (inside) {
-		// too many slots for shared memory: merge this pixel's own lists (one
-		// list per patch offset p), smallest slot number first
-		const int NL = px * px * pt;
-		unsigned cur[kMaxSpc], end[kMaxSpc];
-		for (int l = 0; l < NL; l++) {
-			const int dx = l % px, dy = (l / px) % px, dt = l / (px * px);
-			const int r = ((pt - 1 - dt) * RY + (ly + px - 1 - dy)) * RX + (lx + px - 1 - dx);
-			cur[l] = s_start[r];
-			end[l] = s_start[r] + s_len[r];
-		}
+		// merge by slot number (slots are unique across lists)
 		for (;;) {
 			unsigned best = 0xffffffffu;
 			int bl = -1;
-			for (int l = 0; l < NL; l++)
-				if (cur[l] < end[l]) {
-					const unsigned s = list[cur[l]];
-					if (s < best) { best = s; bl = l; }
-				}
+#pragma unroll
+			for (int l = 0; l < L; l++)
+				if ((PX > 0 || l < nl) && head[l] < best) { best = head[l]; bl = l; }
 			if (bl < 0) break;
-			cur[bl]++;
-			const float *v = vals + (size_t)best * (C * spc);
-			for (int c = 0; c < C; c++) a[c] = __fadd_rn(a[c], v[c * spc + bl]);
-			wa = __fadd_rn(wa, __fmul_rn(wslot[best], s_win[bl]));
+#pragma unroll
+			for (int l = 0; l < L; l++)
+				if (l == bl) {
+					sl[o++] = best << 6 | tag[l];
+					head[l] = ++cur[l] < end[l] ? list[cur[l]] : 0xffffffffu;
+				}
 		}
 	}
-	if (inside) {
+}
+
+// Ordered gather: each pixel merges the spatial lists of the pt origin frames
+// that cover it and adds the terms in slot order -- the order in which the
+// reference's scatter loop adds them.  PT > 0 keeps the pt list heads in
+// registers.
+template <int PT>
+__global__ void gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi,
+                                    const unsigned *__restrict__ soff, const unsigned *__restrict__ sl,
+                                    const float *__restrict__ vals, const float *__restrict__ wslot,
+                                    const float *__restrict__ win, float *__restrict__ acc,
+                                    float *__restrict__ wacc)
+{
+	constexpr int L = PT > 0 ? PT : kMaxSpc;
+	const int px = sp.px, pt = PT > 0 ? PT : sp.pt, spc = sp.spc, C = sp.C;
+	const size_t wh = (size_t)T.w * T.h;
+	const size_t n = wh * (size_t)(f_hi - f_lo + 1);
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+		const int t = f_lo + (int)(i / wh);
+		const size_t xy = i % wh;
+		unsigned cur[L], end[L], head[L];
+		bool any = false;
+#pragma unroll
+		for (int dt = 0; dt < L; dt++) {
+			head[dt] = 0xffffffffu;
+			cur[dt] = end[dt] = 0;
+			const int to = t - dt;
+			if (dt < pt && to >= 0 && to <= sp.F - pt) {
+				const size_t q = (size_t)to * wh + xy;
+				cur[dt] = soff[q];
+				end[dt] = soff[q + 1];
+				if (cur[dt] < end[dt]) { head[dt] = sl[cur[dt]]; any = true; }
+			}
+		}
+		if (!any) continue;
+		const size_t pix = (size_t)t * wh + xy;
+		float a[4] = {0.f, 0.f, 0.f, 0.f};
+		for (int c = 0; c < C; c++) a[c] = acc[((size_t)t * C + c) * wh + xy];
+		float wa = wacc[pix];
+		for (;;) {
+			unsigned best = 0xffffffffu;
+			int bl = -1;
+#pragma unroll
+			for (int l = 0; l < L; l++)
+				if (head[l] < best) { best = head[l]; bl = l; }
+			if (bl < 0) break;
+#pragma unroll
+			for (int l = 0; l < L; l++)
+				if (l == bl) head[l] = ++cur[l] < end[l] ? sl[cur[l]] : 0xffffffffu;
+			const unsigned slot = best >> 6;
+			const int dx = best & 7, dy = (best >> 3) & 7;
+			const int p = (bl * px + dy) * px + dx;
+			const float *v = vals + (size_t)slot * (C * spc) + p;
+			for (int c = 0; c < C; c++) a[c] = __fadd_rn(a[c], v[c * spc]);
+			wa = __fadd_rn(wa, __fmul_rn(wslot[slot], win[p]));
+		}
 		wacc[pix] = wa;
-		for (int c = 0; c < C; c++) acc[(((size_t)t * C + c) * T.h + y) * T.w + x] = a[c];
+		for (int c = 0; c < C; c++) acc[((size_t)t * C + c) * wh + xy] = a[c];
 	}
 }
 
@@ -460,21 +481,34 @@ cudaError_t launch_lists(long long ga, long long gb, int np, const uint8_t *nsim
 	return cudaGetLastError();
 }
 
-cudaError_t launch_gather(const Tile &T, const StepParams &sp, int f_lo, int f_hi, const unsigned *off,
-                          const unsigned *list, const float *vals, const float *wslot, const float *win,
-                          float *acc, float *wacc, cudaStream_t st)
+cudaError_t launch_gather(const Tile &T, const StepParams &sp, int t_lo, int t_hi, const unsigned *off,
+                          const unsigned *list, unsigned *soff, unsigned *sl, unsigned *scratch,
+                          const float *vals, const float *wslot, const float *win, float *acc, float *wacc,
+                          cudaStream_t st)
 {
-	if (f_hi < f_lo) return cudaSuccess;
-	dim3 grid((T.w + kGatherBX - 1) / kGatherBX, (T.h + kGatherBY - 1) / kGatherBY, f_hi - f_lo + 1);
-	gather_kernel<<<grid, kGatherThreads, 0, st>>>(T, sp, f_lo, off, list, vals, wslot, win, acc, wacc);
+	// origin frames [t_lo, t_hi] hold the chunk's member patches; pixels of
+	// frames [t_lo, t_hi + pt - 1] receive them
+	if (t_hi < t_lo) return cudaSuccess;
+	const size_t npos = (size_t)T.w * T.h * sp.F;
+	const int b = grid_for((long long)npos, 256, 16384);
+	slist_count_kernel<<<b, 256, 0, st>>>(T.w, T.h, sp.F, sp.px, sp.pt, t_lo, t_hi, off, soff);
+	cudaError_t e = exclusive_scan(soff, npos, scratch, st);
+	if (e != cudaSuccess) return e;
+	if (sp.px == 4)
+		slist_build_kernel<4><<<b, 256, 0, st>>>(T.w, T.h, sp.F, sp.px, sp.pt, t_lo, t_hi, off, list, soff, sl);
+	else
+		slist_build_kernel<0><<<b, 256, 0, st>>>(T.w, T.h, sp.F, sp.px, sp.pt, t_lo, t_hi, off, list, soff, sl);
+	const int f_hi = t_hi + sp.pt - 1 < sp.F - 1 ? t_hi + sp.pt - 1 : sp.F - 1;
+	const long long npix = (long long)T.w * T.h * (f_hi - t_lo + 1);
+	const int gb = grid_for(npix, 128, 65535);
+	switch (sp.pt) {
+	case 1: gather_slist_kernel<1><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
+	case 2: gather_slist_kernel<2><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
+	case 4: gather_slist_kernel<4><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
+	default: gather_slist_kernel<0><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
+	}
 	return cudaGetLastError();
 }
-
-int gather_region(const StepParams &sp)
-{
-	return (kGatherBX + sp.px - 1) * (kGatherBY + sp.px - 1) * sp.pt;
-}
-int gather_region_max() { return kRegionMax; }
 
 cudaError_t launch_color(const Image &in, const Image &out, int forward, cudaStream_t st)
 {

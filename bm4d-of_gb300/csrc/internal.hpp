@@ -50,12 +50,13 @@ cudaError_t exclusive_scan(unsigned *data, size_t n, unsigned *scratch, cudaStre
 cudaError_t launch_lists(long long ga, long long gb, int np, const uint8_t *nsimp,
                          const uint32_t *idx, const uint8_t *alive, size_t npos, unsigned *cnt,
                          unsigned *off, unsigned *list, unsigned *scratch, cudaStream_t st);
-cudaError_t launch_gather(const Tile &T, const StepParams &sp, int f_lo, int f_hi,
-                          const unsigned *off, const unsigned *list, const float *vals,
-                          const float *wslot, const float *win, float *acc, float *wacc,
-                          cudaStream_t st);
-int gather_region(const StepParams &sp);
-int gather_region_max();
+// Ordered gather of the slots whose origins lie in frames [t_lo, t_hi]:
+// spatial lists (soff: npos+1 entries, sl: px*px entries per slot), then the
+// per-pixel merge over origin frames.
+cudaError_t launch_gather(const Tile &T, const StepParams &sp, int t_lo, int t_hi,
+                          const unsigned *off, const unsigned *list, unsigned *soff, unsigned *sl,
+                          unsigned *scratch, const float *vals, const float *wslot, const float *win,
+                          float *acc, float *wacc, cudaStream_t st);
 cudaError_t launch_color(const Image &in, const Image &out, int forward, cudaStream_t st);
 cudaError_t launch_finalize(const Tile *tiles, int nW, int wTmp, int hTmp, const StepParams &sp,
                             const Image &noisy, const float *acc, const float *wacc,

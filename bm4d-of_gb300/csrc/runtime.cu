@@ -233,7 +233,6 @@ bm4dof_status check_params(const bm4dof_params &p)
 	else if (spc > (unsigned)kMaxSpc) why = "sizePatch^2 * sizePatchTime must be at most 64";
 	else if (p.sizeSearchWindow == 0) why = "sizeSearchWindow must be positive";
 	else if (p.sizeSearchTimeRangeFwd + p.sizeSearchTimeRangeBwd + 1 > (unsigned)kMaxFrames) why = "temporal search range too long";
-	else if ((8 + p.sizePatch - 1) * (8 + p.sizePatch - 1) * p.sizePatchTime > (unsigned)gather_region_max()) why = "patch too large for the aggregation gather";
 	else if (p.doPasteBoost) why = "doPasteBoost is not supported";
 	else if (p.orderInvariance) why = "orderInvariance is not supported";
 	else if (p.sigma <= 0.f) why = "sigma must be positive";
@@ -356,23 +355,28 @@ bm4dof_status run_step(bm4dof_ctx *ctx, int step, const bm4dof_params &p, const 
 	DBUF("wacc", pl.pix, d_wacc);
 	CK(cudaMemsetAsync(d_acc, 0, sizeof(float) * pl.pix * C, st));
 	CK(cudaMemsetAsync(d_wacc, 0, sizeof(float) * pl.pix, st));
-	unsigned *d_cnt, *d_off, *d_scratch;
+	unsigned *d_cnt, *d_off, *d_soff, *d_scratch;
 	DBUF("cnt", pl.maxpos, d_cnt);
 	DBUF("off", pl.maxpos + 1, d_off);
+	DBUF("soff", pl.maxpos + 1, d_soff);
 	DBUF("scratch", pl.maxpos / 4096 + pl.maxpos / (4096ull * 4096ull) + 64, d_scratch);
 
-	const size_t per_group = (size_t)sp.np * ((size_t)C * sp.spc + 2) * sizeof(float);
+	// chunk of groups whose slot terms (vals), weights, origin lists and
+	// spatial lists fit the slot budget; slot numbers must fit 26 bits
+	const size_t per_group = (size_t)sp.np * ((size_t)C * sp.spc + 2 + (size_t)sp.px * sp.px) * sizeof(float);
 	size_t budget = (size_t)16384 << 20;
 	if (const char *env = std::getenv("BM4DOF_SLOT_MB")) budget = (size_t)std::atoll(env) << 20;
 	size_t freeb = 0, totalb = 0;
 	if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess && budget > freeb / 2) budget = freeb / 2;
 	long long chunk = std::max<long long>(1, (long long)(budget / per_group));
+	chunk = std::min<long long>(chunk, ((1ll << 26) - 1) / sp.np);
 	chunk = std::min<long long>(chunk, std::max<long long>(1, G));
 	float *d_vals, *d_wslot;
-	unsigned *d_list;
+	unsigned *d_list, *d_sl;
 	DBUF("vals", (size_t)chunk * sp.np * C * sp.spc, d_vals);
 	DBUF("wslot", (size_t)chunk * sp.np, d_wslot);
 	DBUF("list", (size_t)chunk * sp.np, d_list);
+	DBUF("slist", (size_t)chunk * sp.np * sp.px * sp.px, d_sl);
 
 	for (int ti = 0; ti < ntiles; ti++) {
 		const Tile &T = pl.tiles[ti];
@@ -392,16 +396,17 @@ bm4dof_status run_step(bm4dof_ctx *ctx, int step, const bm4dof_params &p, const 
 				CK(launch_lists(ga, gb, sp.np, d_nsimp, tidx, d_alive, npos, d_cnt, d_off, d_list,
 				                d_scratch, st));
 				ctx->launches += 5;
-				// frames that the chunk's member patches can touch
+				// origin frames of the chunk's member patches: the temporal search
+				// range of a reference frame t lies within t -/+ (wtb + wtf)
 				const long long fa = (ga - T.g0) / ((long long)T.nx * T.ny);
 				const long long fb = (gb - 1 - T.g0) / ((long long)T.nx * T.ny);
 				const int ta = pl.grid[T.gf + (int)fa], tb = pl.grid[T.gf + (int)fb];
 				const int reach = sp.wtb + sp.wtf;
-				const int f_lo = std::max(0, ta - reach);
-				const int f_hi = std::min((int)F - 1, tb + reach + sp.pt - 1);
-				CK(launch_gather(T, sp, f_lo, f_hi, d_off, d_list, d_vals, d_wslot, d_win,
-				                 d_acc + T.pix0 * C, d_wacc + T.pix0, st));
-				ctx->launches++;
+				const int t_lo = std::max(0, ta - reach);
+				const int t_hi = std::min((int)F - sp.pt, tb + reach);
+				CK(launch_gather(T, sp, t_lo, t_hi, d_off, d_list, d_soff, d_sl, d_scratch, d_vals, d_wslot,
+				                 d_win, d_acc + T.pix0 * C, d_wacc + T.pix0, st));
+				ctx->launches += 4;
 			}
 		}
 	}
