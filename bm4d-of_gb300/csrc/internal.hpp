@@ -23,10 +23,12 @@ bool make_basis(int transform, unsigned px, unsigned pt, std::vector<float> &bas
 std::vector<float> make_window(bool agg, unsigned px, unsigned pt);
 
 // search.cu
-size_t search_smem_bytes(const StepParams &sp);
-cudaError_t launch_search(const Image &src, const Image &ffl, const Image &bfl, const Tile *tiles,
-                          int ntiles, const int *grid, const StepParams &sp, long long g_begin,
-                          long long g_end, uint8_t *nsimp, uint32_t *idx, int nsm, cudaStream_t st);
+int search_frames_max(const StepParams &sp);
+cudaError_t launch_traj(const Image &ffl, const Image &bfl, const Tile *tiles, int ntiles, const int *grid,
+                        const StepParams &sp, long long G, uint32_t *traj, cudaStream_t st);
+cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const int *grid,
+                          const uint32_t *traj, const StepParams &sp, long long g_begin, long long g_end,
+                          uint8_t *nsimp, uint32_t *idx, int *err, int nsm, cudaStream_t st);
 
 // filter.cu
 size_t filter_smem_bytes(const StepParams &sp);

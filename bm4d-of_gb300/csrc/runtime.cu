@@ -306,21 +306,33 @@ bm4dof_status run_step(bm4dof_ctx *ctx, int step, const bm4dof_params &p, const 
 	DBUF("killed", G, d_killed);
 	DBUF("idx", (size_t)G * sp.np, d_idx);
 	DBUF("wgroup", G, d_wgroup);
-	DBUF("small", 64 + ntiles, d_small);   // [0] edge count, [1] changed, [2..] per-tile counts
+	// [0] edge count, [1] changed flag, [2] search wait-timeout flag,
+	// [64 ..] per-tile processed-group counts
+	DBUF("small", 64 + ntiles, d_small);
+	uint32_t *d_traj;
+	DBUF("traj", (size_t)G * search_frames_max(sp), d_traj);
+	CK(cudaMemsetAsync(d_small, 0, sizeof(unsigned) * (64 + ntiles), st));
 
 	// ---- patch search of every group -------------------------------------
 	{
 		Mark m(ctx, T_SEARCH);
-		CK(launch_search(step == 1 ? noisy : basic, ffl, bfl, d_tiles, ntiles, d_grid, sp, 0, G,
-		                 d_nsimp, d_idx, ctx->nsm, st));
-		ctx->launches++;
+		CK(launch_traj(ffl, bfl, d_tiles, ntiles, d_grid, sp, G, d_traj, st));
+		CK(launch_search(step == 1 ? noisy : basic, d_tiles, ntiles, d_grid, d_traj, sp, 0, G, d_nsimp, d_idx,
+		                 reinterpret_cast<int *>(d_small + 2), ctx->nsm, st));
+		ctx->launches += 2;
 	}
 
 	// ---- mask switch-offs (rare): killer -> victim edges, then fixed point --
 	{
 		Mark m(ctx, T_OTHER);
 		CK(cudaMemsetAsync(d_alive, 1, G, st));
-		CK(cudaMemsetAsync(d_small, 0, sizeof(unsigned) * (64 + ntiles), st));
+		unsigned timeout = 0;
+		CK(cudaMemcpyAsync(&timeout, d_small + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		if (timeout) {
+			set_error("bm4dof: a shared-memory window load did not complete (bounded wait expired)");
+			return BM4DOF_ERR_TIMEOUT;
+		}
 		unsigned cap = 1u << 16;
 		unsigned long long *d_edges;
 		DBUF("edges", cap, d_edges);
@@ -345,7 +357,7 @@ bm4dof_status run_step(bm4dof_ctx *ctx, int step, const bm4dof_params &p, const 
 			CK(cudaStreamSynchronize(st));
 			if (!changed) break;
 		}
-		CK(launch_count_alive(d_tiles, ntiles, G, d_alive, d_small + 2, st));
+		CK(launch_count_alive(d_tiles, ntiles, G, d_alive, d_small + 64, st));
 		ctx->launches++;
 	}
 
@@ -420,7 +432,7 @@ bm4dof_status run_step(bm4dof_ctx *ctx, int step, const bm4dof_params &p, const 
 	}
 
 	std::vector<unsigned> counts(ntiles);
-	CK(cudaMemcpyAsync(counts.data(), d_small + 2, sizeof(unsigned) * ntiles, cudaMemcpyDeviceToHost, st));
+	CK(cudaMemcpyAsync(counts.data(), d_small + 64, sizeof(unsigned) * ntiles, cudaMemcpyDeviceToHost, st));
 	CK(cudaStreamSynchronize(st));
 	const float whf = (float)(W * H * F);
 	for (int n = 0; n < ntiles; n++) *ratio += 100.f * (float)counts[n] / whf;   // nldct.cpp:403-404
