@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 #include <cstdint>
+#include <cstring>
 
 #include "common.cuh"
 #include "internal.hpp"
@@ -37,7 +38,7 @@ namespace bm4dof {
 
 namespace {
 
-constexpr int kThreads = 64;
+constexpr int kThreads = 288;          // 9 warps: 567 strips of a 21x21x9 window set in 2 rounds
 constexpr int kSW = 7;                 // candidates per thread along x
 constexpr unsigned kWaitLimit = 1u << 24;
 
@@ -248,11 +249,14 @@ __device__ void plan_group(const SearchArgs &a, const StepParams &sp, long long 
 	(void)nstrip_w;
 }
 
-// Distances of kSW adjacent candidates from a window row block in shared
-// memory.  REFREG: reference patch in registers (one channel, PX*PX*PT values).
+// Distances of kSW horizontally adjacent candidates.  The window rows come
+// from shared memory (STAGE: the frame's TMA box, row pitch BX) or straight
+// from the video in global memory.  REFREG: the reference patch (one channel,
+// PX*PX*PT values) lives in registers, else in shared memory.
 template <int PX, int PT, bool REFREG>
-__device__ __forceinline__ void strip_distances(const float *win, int BX, int BY, int CB, int chn, int xs,
-                                                int ys, int px_rt, int pt_rt, const float *ref_s,
+__device__ __forceinline__ void strip_distances(const float *base, size_t rpitch, size_t cpitch, size_t tpitch,
+                                                int xs, int xmax, int chn, int px_rt, int pt_rt,
+                                                const float *ref_s,
                                                 const float (&ref_r)[(PX > 0 ? PX * PX * PT : 1)],
                                                 float acc[kSW])
 {
@@ -268,10 +272,10 @@ __device__ __forceinline__ void strip_distances(const float *win, int BX, int BY
 			for (int ht = 0; ht < (PT > 0 ? PT : 1); ht++)
 #pragma unroll
 				for (int hy = 0; hy < PX; hy++) {
-					const float *row = win + ((ht * CB + c) * BY + ys + hy) * BX;
+					const float *row = base + ht * tpitch + c * cpitch + hy * rpitch;
 					float v[NV];
 #pragma unroll
-					for (int j = 0; j < NV; j++) v[j] = row[min(xs + j, BX - 1)];
+					for (int j = 0; j < NV; j++) v[j] = row[min(xs + j, xmax)];
 #pragma unroll
 					for (int hx = 0; hx < PX; hx++) {
 						const int kk = (ht * PX + hy) * PX + hx;
@@ -288,12 +292,12 @@ __device__ __forceinline__ void strip_distances(const float *win, int BX, int BY
 		for (int c = 0; c < chn; c++)
 			for (int ht = 0; ht < pt; ht++)
 				for (int hy = 0; hy < px; hy++) {
-					const float *row = win + ((ht * CB + c) * BY + ys + hy) * BX;
+					const float *row = base + ht * tpitch + c * cpitch + hy * rpitch;
 					for (int hx = 0; hx < px; hx++, k++) {
 						const float r = ref_s[k];
 #pragma unroll
 						for (int j = 0; j < kSW; j++) {
-							const float d = __fsub_rn(r, row[min(xs + j + hx, BX - 1)]);
+							const float d = __fsub_rn(r, row[min(xs + j + hx, xmax)]);
 							acc[j] = __fadd_rn(acc[j], __fmul_rn(d, d));
 						}
 					}
@@ -301,89 +305,180 @@ __device__ __forceinline__ void strip_distances(const float *win, int BX, int BY
 	}
 }
 
-// Window stream of one CTA: the frames of its groups in processing order,
-// each loaded by TMA into one of two buffers (FIFO).  Thread 0 keeps the
-// issue cursor; it runs at most one group ahead of the group being computed,
-// whose window table lives in the other plan slot.
-struct IssueState {
-	long long ig;     // group of the next window to request
-	int ifr;          // its frame index
-	int islot;        // plan slot of that group
-	int inflight;     // windows requested and not yet consumed
-	unsigned issued;  // windows requested so far
+struct SelectShared {
+	unsigned hist[256];
+	unsigned prefix, rank, count_eq, nsel;
+	int fallback;
+	float sd[kMaxNp];
+	int si[kMaxNp];
+	float hd[kMaxNp];
+	int hi[kMaxNp];
 };
 
-template <int PX, int PT, bool REFREG>
+// The k nearest of dist[0..ncand) in std::partial_sort's output order.
+//  Fast path (all threads): radix select of the k-th distance on the float bit
+//  patterns (distances are >= +0, so bit order is value order).  When the k
+//  smallest are strictly below every other distance and pairwise distinct,
+//  partial_sort's output is the unique ascending order of that set, which one
+//  warp sorts.  Otherwise (exact ties) warp 0 replays libstdc++'s heap
+//  selection (__heap_select then __sort_heap) on the candidates in order.
+//  Results land in S.sd / S.si (sorted) for the first K entries.
+__device__ void select_knn(const float *dist, int ncand, int K, SelectShared &S)
+{
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	if (tid == 0) { S.prefix = 0u; S.rank = (unsigned)K; S.nsel = 0u; S.fallback = 0; }
+	for (int pass = 0; pass < 4; pass++) {
+		const int shift = 24 - 8 * pass;
+		for (int b = tid; b < 256; b += blockDim.x) S.hist[b] = 0u;
+		__syncthreads();
+		const unsigned pre = S.prefix;
+		for (int i = tid; i < ncand; i += blockDim.x) {
+			const unsigned key = __float_as_uint(dist[i]);
+			if (pass == 0 || (key >> (shift + 8)) == (pre >> (shift + 8))) atomicAdd(&S.hist[(key >> shift) & 255u], 1u);
+		}
+		__syncthreads();
+		if (warp == 0) {
+			unsigned c[8], run = 0;
+#pragma unroll
+			for (int j = 0; j < 8; j++) { c[j] = S.hist[lane * 8 + j]; run += c[j]; }
+			unsigned inc = run;
+#pragma unroll
+			for (int o = 1; o < 32; o <<= 1) {
+				const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
+				if (lane >= o) inc += v;
+			}
+			const unsigned excl = inc - run, rank = S.rank;
+			const unsigned ball = __ballot_sync(0xffffffffu, inc >= rank);
+			const int first = __ffs(ball) - 1;
+			if (lane == first) {
+				unsigned cum = excl;
+				int b = 0;
+				while (cum + c[b] < rank) { cum += c[b]; b++; }
+				S.prefix = pre | ((unsigned)(lane * 8 + b) << shift);
+				S.rank = rank - cum;
+				S.count_eq = c[b];
+			}
+		}
+		__syncthreads();
+	}
+	// unique boundary: exactly K distances are <= the k-th one
+	const unsigned T = S.prefix;
+	const bool unique = S.count_eq == S.rank;
+	if (unique) {
+		for (int i = tid; i < ncand; i += blockDim.x)
+			if (__float_as_uint(dist[i]) <= T) {
+				const unsigned s = atomicAdd(&S.nsel, 1u);
+				if (s < (unsigned)kMaxNp) { S.sd[s] = dist[i]; S.si[s] = i; }
+			}
+	}
+	__syncthreads();
+	if (warp == 0) {
+		bool ok = unique && S.nsel == (unsigned)K;
+		if (ok) {
+			// bitonic sort of K <= 32 (distance, candidate) pairs across the warp
+			float d = lane < K ? S.sd[lane] : __int_as_float(0x7f800000);
+			int ix = lane < K ? S.si[lane] : 0x7fffffff;
+			for (int k = 2; k <= 32; k <<= 1)
+				for (int j = k >> 1; j > 0; j >>= 1) {
+					const float od = __shfl_xor_sync(0xffffffffu, d, j);
+					const int oi = __shfl_xor_sync(0xffffffffu, ix, j);
+					const bool up = (lane & k) == 0, low = (lane & j) == 0;
+					const bool take = (low == up) ? (od < d || (od == d && oi < ix)) : (od > d || (od == d && oi > ix));
+					if (take) { d = od; ix = oi; }
+				}
+			const float nd = __shfl_down_sync(0xffffffffu, d, 1);
+			const bool tie = lane + 1 < K && nd == d;
+			ok = __ballot_sync(0xffffffffu, tie) == 0u;
+			if (ok && lane < K) { S.sd[lane] = d; S.si[lane] = ix; }
+		}
+		if (!ok) {
+			// exact replay of libstdc++'s heap selection, candidates in order
+			float *hd = S.hd;
+			int *hi = S.hi;
+			if (lane == 0) {
+				for (int i = 0; i < K; i++) { hd[i] = dist[i]; hi[i] = i; }
+				make_heap(hd, hi, K);
+			}
+			__syncwarp();
+			float top = hd[0];
+			for (int base = K; base < ncand; base += 32) {
+				const int i = base + lane;
+				const float dv = i < ncand ? dist[i] : 0.f;
+				unsigned m = __ballot_sync(0xffffffffu, i < ncand && dv < top);
+				while (m) {
+					const int j = __ffs(m) - 1;
+					if (lane == 0) adjust_heap(hd, hi, 0, K, dist[base + j], base + j);
+					__syncwarp();
+					top = hd[0];
+					m &= ~((2u << j) - 1u);
+					m &= __ballot_sync(0xffffffffu, i < ncand && dv < top);
+				}
+			}
+			if (lane == 0) {
+				sort_heap(hd, hi, K);
+				for (int i = 0; i < K; i++) { S.sd[i] = hd[i]; S.si[i] = hi[i]; }
+			}
+		}
+	}
+	__syncthreads();
+}
+
+// One CTA handles one group at a time.  STAGE: every frame window of the group
+// is requested by TMA at once (one buffer and one mbarrier per frame); the
+// next group's windows are requested right after the distances are done, so
+// the loads overlap the k-nearest selection.
+template <int PX, int PT, bool REFREG, bool STAGE>
 __global__ void __launch_bounds__(kThreads)
 search_kernel(const __grid_constant__ CUtensorMap map, Image src, StepParams sp, SearchArgs a)
 {
 	extern __shared__ __align__(128) unsigned char smem_raw[];
-	const int box = a.BX * a.BY * a.CB * sp.pt;              // floats per window buffer
+	const int box = a.BX * a.BY * a.CB * sp.pt;               // floats per window buffer
 	const int boxp = (box + 31) / 32 * 32;
-	float *bufs[2] = {reinterpret_cast<float *>(smem_raw), reinterpret_cast<float *>(smem_raw) + boxp};
-	float *dist = bufs[1] + boxp;
-	const int ncand_max = sp.wx * sp.wx * (sp.wtf + sp.wtb + 1);
-	float *ref_s = dist + ncand_max;                           // chn * spc
+	float *wins = reinterpret_cast<float *>(smem_raw);
+	float *dist = wins + (STAGE ? (size_t)boxp * a.nfm : 0);
+	const int ncand_max = sp.wx * sp.wx * a.nfm;
+	float *ref_s = dist + ncand_max;                            // chn * spc
 	__shared__ FrameWin fw[2][kMaxFrames];
 	__shared__ int s_nframes[2], s_ncand[2], s_nitems[2], s_tile[2], s_x[2], s_y[2], s_t[2];
-	__shared__ float hd[kMaxNp];
-	__shared__ int hi[kMaxNp];
-	__shared__ __align__(8) uint64_t bars[2];
+	__shared__ __align__(8) uint64_t bars[kMaxFrames];
+	__shared__ unsigned s_phase[kMaxFrames];
 	__shared__ int s_abort;
+	__shared__ SelectShared S;
 
-	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int tid = threadIdx.x;
 	const int chn = sp.chn_search;
 	const unsigned box_bytes = (unsigned)box * 4u;
-	IssueState is = {0, 0, 0, 0, 0u};   // meaningful in thread 0 only
-	int cur = 0;
 
-	auto issue_more = [&]() {
-		while (is.inflight < 2 && is.ig < a.g_end) {
-			if (is.ifr >= s_nframes[is.islot]) {
-				// next group of this CTA: only into the slot not being computed
-				if (is.islot != cur) break;
-				is.ig += gridDim.x;
-				if (is.ig >= a.g_end) break;
-				is.islot ^= 1;
-				is.ifr = 0;
-				const int sl = is.islot;
-				plan_group(a, sp, is.ig, fw[sl], s_nframes[sl], s_ncand[sl], s_nitems[sl], s_tile[sl], s_x[sl],
-				           s_y[sl], s_t[sl], 0);
-				continue;
-			}
-			const FrameWin &f = fw[is.islot][is.ifr];
-			const int b = is.issued & 1;
-			mbar_expect_tx(&bars[b], box_bytes);
-			tma_load_4d(bufs[b], &map, &bars[b], f.X0, a.tiles[s_tile[is.islot]].oy + f.ry0, 0, f.qt);
-			is.issued++;
-			is.ifr++;
-			is.inflight++;
+	auto request = [&](int slot) {
+		// thread 0: TMA loads of every frame window of the group planned in slot
+		const Tile T = a.tiles[s_tile[slot]];
+		for (int ii = 0; ii < s_nframes[slot]; ii++) {
+			const FrameWin &f = fw[slot][ii];
+			mbar_expect_tx(&bars[ii], box_bytes);
+			tma_load_4d(wins + (size_t)ii * boxp, &map, &bars[ii], f.X0, T.oy + f.ry0, 0, f.qt);
+			s_phase[ii]++;
 		}
 	};
 
+	int cur = 0;
+	long long g = a.g_begin + blockIdx.x;
 	if (tid == 0) {
-		mbar_init(&bars[0], 1);
-		mbar_init(&bars[1], 1);
-		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		s_abort = 0;
-		is.ig = a.g_begin + blockIdx.x;
-		is.ifr = 0;
-		is.islot = 0;
-		is.inflight = 0;
-		is.issued = 0;
-		if (is.ig < a.g_end) {
-			plan_group(a, sp, is.ig, fw[0], s_nframes[0], s_ncand[0], s_nitems[0], s_tile[0], s_x[0], s_y[0],
-			           s_t[0], 0);
-			issue_more();
+		for (int ii = 0; ii < kMaxFrames; ii++) s_phase[ii] = 0u;
+		if (STAGE) {
+			for (int ii = 0; ii < a.nfm; ii++) mbar_init(&bars[ii], 1);
+			asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		}
+		if (g < a.g_end) {
+			plan_group(a, sp, g, fw[0], s_nframes[0], s_ncand[0], s_nitems[0], s_tile[0], s_x[0], s_y[0], s_t[0], 0);
+			if (STAGE) request(0);
 		}
 	}
 	__syncthreads();
 
-	unsigned consumed = 0;
-	for (long long g = a.g_begin + blockIdx.x; g < a.g_end; g += gridDim.x) {
+	for (; g < a.g_end; g += gridDim.x) {
 		const Tile T = a.tiles[s_tile[cur]];
 		const int nframes = s_nframes[cur];
-		// reference patch, channel-major (c, ht, hy, hx)
 		float ref_r[(PX > 0 ? PX * PX * PT : 1)];
 		if (REFREG) {
 #pragma unroll
@@ -401,83 +496,74 @@ search_kernel(const __grid_constant__ CUtensorMap map, Image src, StepParams sp,
 			__syncthreads();
 		}
 
-		for (int ii = 0; ii < nframes; ii++, consumed++) {
-			const int b = consumed & 1;
-			const unsigned parity = (consumed >> 1) & 1u;
-			// bounded wait for this frame's window (every thread observes the phase)
-			unsigned n = 0;
-			while (!mbar_try_wait(&bars[b], parity))
-				if (++n > kWaitLimit) { s_abort = 1; atomicExch(a.err, 1); break; }
-			__syncthreads();
-			if (s_abort) return;
+		// distances of every candidate, stored in the reference's candidate order
+		const int nit = s_nitems[cur];
+		int ii = 0;
+		for (int it = tid; it < nit; it += blockDim.x) {
+			while (ii + 1 < nframes && fw[cur][ii + 1].ibase <= it) ii++;
 			const FrameWin f = fw[cur][ii];
-			const float *win = bufs[b];
-			const int nstrip = (f.nx + kSW - 1) / kSW;
-			const int nit = f.ny * nstrip;
-			for (int it = tid; it < nit; it += blockDim.x) {
-				const int row = it / nstrip, strip = it - row * nstrip;
-				float acc[kSW];
-				strip_distances<PX, PT, REFREG>(win, a.BX, a.BY, a.CB, chn, f.xoff + strip * kSW, row, sp.px, sp.pt,
-				                                ref_s, ref_r, acc);
-				float *dd = dist + f.cbase + row * f.nx + strip * kSW;
-#pragma unroll
-				for (int j = 0; j < kSW; j++)
-					if (strip * kSW + j < f.nx) dd[j] = acc[j];
+			if (STAGE) {
+				// bounded wait for this frame's window
+				const unsigned parity = (s_phase[ii] - 1u) & 1u;
+				unsigned n = 0;
+				while (!mbar_try_wait(&bars[ii], parity))
+					if (++n > kWaitLimit) { s_abort = 1; atomicExch(a.err, 1); break; }
+				if (s_abort) break;
 			}
-			__syncthreads();
-			if (tid == 0) {
-				// the buffer just read may be refilled by the async proxy
+			const int nstrip = (f.nx + kSW - 1) / kSW;
+			const int rel = it - f.ibase;
+			const int row = rel / nstrip, strip = rel - row * nstrip;
+			float acc[kSW];
+			if (STAGE) {
+				const float *base = wins + (size_t)ii * boxp + (size_t)row * a.BX;
+				strip_distances<PX, PT, REFREG>(base, a.BX, (size_t)a.BX * a.BY, (size_t)a.BX * a.BY * a.CB,
+				                                f.xoff + strip * kSW, a.BX - 1, chn, sp.px, sp.pt, ref_s, ref_r, acc);
+			} else {
+				const float *base = src.p + src.at(0, T.oy + f.ry0 + row, f.qt, 0);
+				strip_distances<PX, PT, REFREG>(base, src.P, src.plane(), src.plane() * src.C,
+				                                T.ox + f.rx0 + strip * kSW, T.ox + T.w - 1, chn, sp.px, sp.pt,
+				                                ref_s, ref_r, acc);
+			}
+			float *dd = dist + f.cbase + row * f.nx + strip * kSW;
+#pragma unroll
+			for (int j = 0; j < kSW; j++)
+				if (strip * kSW + j < f.nx) dd[j] = acc[j];
+		}
+		__syncthreads();
+		if (s_abort) return;
+
+		// plan the next group and request its windows: they load during the selection
+		if (tid == 0 && g + gridDim.x < a.g_end) {
+			const int sl = cur ^ 1;
+			plan_group(a, sp, g + gridDim.x, fw[sl], s_nframes[sl], s_ncand[sl], s_nitems[sl], s_tile[sl], s_x[sl],
+			           s_y[sl], s_t[sl], 0);
+			if (STAGE) {
 				asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-				is.inflight--;
-				issue_more();
+				request(sl);
 			}
 		}
 
-		// k nearest with the libstdc++ heap selection (warp 0)
-		if (warp == 0) {
-			const int ncand = s_ncand[cur];
-			const int K = min(sp.np, ncand);
-			if (lane == 0) {
-				for (int i = 0; i < K; i++) { hd[i] = dist[i]; hi[i] = i; }
-				make_heap(hd, hi, K);
-			}
-			__syncwarp();
-			float top = hd[0];
-			for (int base = K; base < ncand; base += 32) {
-				const int i = base + lane;
-				const float d = i < ncand ? dist[i] : 0.f;
-				unsigned m = __ballot_sync(0xffffffffu, i < ncand && d < top);
-				while (m) {
-					const int j = __ffs(m) - 1;
-					if (lane == 0) adjust_heap(hd, hi, 0, K, dist[base + j], base + j);
-					__syncwarp();
-					top = hd[0];
-					m &= ~((2u << j) - 1u);
-					m &= __ballot_sync(0xffffffffu, i < ncand && d < top);
-				}
-			}
-			if (lane == 0) {
-				sort_heap(hd, hi, K);
-				int n = 1;
-				while (2 * n <= K && hd[n] < sp.tau2) n *= 2;
-				a.nsimp[g] = (uint8_t)n;
-				for (int q = 0; q < n; q++) {
-					const int c = hi[q];
-					int ii = 0;
-					while (ii + 1 < nframes && fw[cur][ii + 1].cbase <= c) ii++;
-					const FrameWin &f = fw[cur][ii];
-					const int rel = c - f.cbase;
-					const int qy = f.ry0 + rel / f.nx, qx = f.rx0 + rel % f.nx;
-					a.idx[g * sp.np + q] = (uint32_t)(((long long)f.qt * T.h + qy) * T.w + qx);
-				}
+		const int ncand = s_ncand[cur];
+		const int K = min(sp.np, ncand);
+		select_knn(dist, ncand, K, S);
+		if (tid == 0) {
+			int n = 1;
+			while (2 * n <= K && S.sd[n] < sp.tau2) n *= 2;   // nldct.cpp:1284-1289
+			a.nsimp[g] = (uint8_t)n;
+			for (int q = 0; q < n; q++) {
+				const int c = S.si[q];
+				int jj = 0;
+				while (jj + 1 < nframes && fw[cur][jj + 1].cbase <= c) jj++;
+				const FrameWin &f = fw[cur][jj];
+				const int rl = c - f.cbase;
+				const int qy = f.ry0 + rl / f.nx, qx = f.rx0 + rl % f.nx;
+				a.idx[g * sp.np + q] = (uint32_t)(((long long)f.qt * T.h + qy) * T.w + qx);
 			}
 		}
 		__syncthreads();
 		cur ^= 1;
-		if (tid == 0) issue_more();
-		__syncthreads();
 	}
-	// every requested window belongs to a group of this CTA and was consumed
+	// every window requested belongs to a group of this CTA and was waited for
 }
 
 // nSimilarPatches == 1: the group is the reference patch alone (nldct.cpp:1326-1327).
@@ -509,14 +595,19 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 	return fn;
 }
 
-template <int PX, int PT, bool REFREG>
+template <int PX, int PT, bool REFREG, bool STAGE>
 cudaError_t launch_t(const CUtensorMap &map, const Image &src, const StepParams &sp, const SearchArgs &a,
-                     size_t smem, int blocks, cudaStream_t st)
+                     size_t smem, int nsm, long long n, cudaStream_t st)
 {
-	cudaError_t e = cudaFuncSetAttribute(search_kernel<PX, PT, REFREG>,
+	cudaError_t e = cudaFuncSetAttribute(search_kernel<PX, PT, REFREG, STAGE>,
 	                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
-	search_kernel<PX, PT, REFREG><<<blocks, kThreads, smem, st>>>(map, src, sp, a);
+	int per_sm = 0;
+	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, search_kernel<PX, PT, REFREG, STAGE>, kThreads, smem);
+	if (e != cudaSuccess) return e;
+	long long blocks = (long long)nsm * (per_sm < 1 ? 1 : per_sm);
+	if (blocks > n) blocks = n;
+	search_kernel<PX, PT, REFREG, STAGE><<<(int)blocks, kThreads, smem, st>>>(map, src, sp, a);
 	return cudaGetLastError();
 }
 
@@ -559,35 +650,44 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
 	a.nsimp = nsimp;
 	a.idx = idx;
 	a.err = err;
-	if (a.BX > 256 || a.BY > 256 || sp.pt > 256) return cudaErrorInvalidValue;
-
-	PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
-	if (!enc) return cudaErrorNotSupported;
-	CUtensorMap map;
-	const cuuint64_t dims[4] = {(cuuint64_t)src.P, (cuuint64_t)src.H, (cuuint64_t)src.C, (cuuint64_t)src.F};
-	const cuuint64_t strides[3] = {(cuuint64_t)src.P * 4, (cuuint64_t)src.P * src.H * 4,
-	                               (cuuint64_t)src.P * src.H * src.C * 4};
-	const cuuint32_t boxd[4] = {(cuuint32_t)a.BX, (cuuint32_t)a.BY, (cuuint32_t)a.CB, (cuuint32_t)sp.pt};
-	const cuuint32_t estr[4] = {1, 1, 1, 1};
-	CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src.p, dims, strides, boxd, estr,
-	                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-	                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-	if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
-
-	const int box = a.BX * a.BY * a.CB * sp.pt;
-	const int boxp = (box + 31) / 32 * 32;
-	const int ncand = sp.wx * sp.wx * (sp.wtf + sp.wtb + 1);
-	const size_t smem = sizeof(float) * (2 * (size_t)boxp + ncand + (size_t)sp.spc * sp.chn_search);
-	if (smem > 220 * 1024) return cudaErrorInvalidValue;
 	const long long n = g_end - g_begin;
-	const int per_sm = (int)((200 * 1024) / (smem + 1024));
-	long long blocks = (long long)nsm * (per_sm < 1 ? 1 : (per_sm > 16 ? 16 : per_sm));
-	if (blocks > n) blocks = n;
-	if (sp.chn_search == 1 && sp.px == 4 && sp.pt == 4) return launch_t<4, 4, true>(map, src, sp, a, smem, (int)blocks, st);
-	if (sp.chn_search == 1 && sp.px == 8 && sp.pt == 1) return launch_t<8, 1, true>(map, src, sp, a, smem, (int)blocks, st);
-	if (sp.px == 4 && sp.pt == 4) return launch_t<4, 4, false>(map, src, sp, a, smem, (int)blocks, st);
-	if (sp.px == 8 && sp.pt == 1) return launch_t<8, 1, false>(map, src, sp, a, smem, (int)blocks, st);
-	return launch_t<0, 0, false>(map, src, sp, a, smem, (int)blocks, st);
+	const int box = a.BX * a.BY * a.CB * sp.pt;
+	const size_t boxp = (size_t)(box + 31) / 32 * 32;
+	const size_t ncand = (size_t)sp.wx * sp.wx * a.nfm;
+	const size_t small = sizeof(float) * (ncand + (size_t)sp.spc * sp.chn_search);
+	const size_t staged = small + sizeof(float) * boxp * a.nfm;
+	const bool stage = a.BX <= 256 && a.BY <= 256 && sp.pt <= 256 && staged <= 110 * 1024;
+
+	CUtensorMap map;
+	std::memset(&map, 0, sizeof(map));
+	if (stage) {
+		PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+		if (!enc) return cudaErrorNotSupported;
+		const cuuint64_t dims[4] = {(cuuint64_t)src.P, (cuuint64_t)src.H, (cuuint64_t)src.C, (cuuint64_t)src.F};
+		const cuuint64_t strides[3] = {(cuuint64_t)src.P * 4, (cuuint64_t)src.P * src.H * 4,
+		                               (cuuint64_t)src.P * src.H * src.C * 4};
+		const cuuint32_t boxd[4] = {(cuuint32_t)a.BX, (cuuint32_t)a.BY, (cuuint32_t)a.CB, (cuuint32_t)sp.pt};
+		const cuuint32_t estr[4] = {1, 1, 1, 1};
+		CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src.p, dims, strides, boxd, estr,
+		                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+		                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+	}
+	const size_t smem = stage ? staged : small;
+	const bool one = sp.chn_search == 1;
+	if (sp.px == 4 && sp.pt == 4) {
+		if (one && stage) return launch_t<4, 4, true, true>(map, src, sp, a, smem, nsm, n, st);
+		if (one) return launch_t<4, 4, true, false>(map, src, sp, a, smem, nsm, n, st);
+		if (stage) return launch_t<4, 4, false, true>(map, src, sp, a, smem, nsm, n, st);
+		return launch_t<4, 4, false, false>(map, src, sp, a, smem, nsm, n, st);
+	}
+	if (sp.px == 8 && sp.pt == 1) {
+		if (one && stage) return launch_t<8, 1, true, true>(map, src, sp, a, smem, nsm, n, st);
+		if (stage) return launch_t<8, 1, false, true>(map, src, sp, a, smem, nsm, n, st);
+		return launch_t<8, 1, false, false>(map, src, sp, a, smem, nsm, n, st);
+	}
+	if (stage) return launch_t<0, 0, false, true>(map, src, sp, a, smem, nsm, n, st);
+	return launch_t<0, 0, false, false>(map, src, sp, a, smem, nsm, n, st);
 }
 
 }  // namespace bm4dof
