@@ -38,7 +38,7 @@ namespace bm4dof {
 
 namespace {
 
-constexpr int kThreads = 288;          // 9 warps: 567 strips of a 21x21x9 window set in 2 rounds
+constexpr int kThreads = 128;
 constexpr int kSW = 7;                 // candidates per thread along x
 constexpr unsigned kWaitLimit = 1u << 24;
 
@@ -305,91 +305,112 @@ __device__ __forceinline__ void strip_distances(const float *base, size_t rpitch
 	}
 }
 
+constexpr int kSelCap = 64;           // candidates the fast selection sorts
+
 struct SelectShared {
-	unsigned hist[256];
-	unsigned prefix, rank, count_eq, nsel;
-	int fallback;
-	float sd[kMaxNp];
-	int si[kMaxNp];
+	float tmin[kThreads];
+	float bound;
+	unsigned nsel;
+	float sd[kSelCap];
+	int si[kSelCap];
 	float hd[kMaxNp];
 	int hi[kMaxNp];
 };
 
-// The k nearest of dist[0..ncand) in std::partial_sort's output order.
-//  Fast path (all threads): radix select of the k-th distance on the float bit
-//  patterns (distances are >= +0, so bit order is value order).  When the k
-//  smallest are strictly below every other distance and pairwise distinct,
-//  partial_sort's output is the unique ascending order of that set, which one
-//  warp sorts.  Otherwise (exact ties) warp 0 replays libstdc++'s heap
-//  selection (__heap_select then __sort_heap) on the candidates in order.
-//  Results land in S.sd / S.si (sorted) for the first K entries.
-__device__ void select_knn(const float *dist, int ncand, int K, SelectShared &S)
+// The k nearest of dist[0..ncand) in std::partial_sort's output order; the
+// first K entries of S.sd / S.si receive them, sorted.
+//
+// Fast path: every thread knows the minimum of the distances it computed; the
+// K-th smallest of those minima bounds the K-th smallest distance from above
+// (they are K distinct candidates).  All candidates under the bound are
+// compacted and one warp sorts them.  When the K smallest are pairwise
+// distinct and strictly below every other distance, partial_sort's output is
+// exactly this ascending order.  Otherwise (exact ties, or too many
+// candidates under the bound) warp 0 replays libstdc++'s heap selection
+// (__heap_select then __sort_heap) over the candidates in order.
+__device__ void select_knn(const float *dist, int ncand, int K, float tmin, SelectShared &S)
 {
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	if (tid == 0) { S.prefix = 0u; S.rank = (unsigned)K; S.nsel = 0u; S.fallback = 0; }
-	for (int pass = 0; pass < 4; pass++) {
-		const int shift = 24 - 8 * pass;
-		for (int b = tid; b < 256; b += blockDim.x) S.hist[b] = 0u;
-		__syncthreads();
-		const unsigned pre = S.prefix;
-		for (int i = tid; i < ncand; i += blockDim.x) {
-			const unsigned key = __float_as_uint(dist[i]);
-			if (pass == 0 || (key >> (shift + 8)) == (pre >> (shift + 8))) atomicAdd(&S.hist[(key >> shift) & 255u], 1u);
-		}
-		__syncthreads();
-		if (warp == 0) {
-			unsigned c[8], run = 0;
+	S.tmin[tid] = tmin;
+	if (tid == 0) S.nsel = 0u;
+	__syncthreads();
+	if (warp == 0) {
+		// K-th smallest of the per-thread minima (repeated warp minimum)
+		constexpr int P = kThreads / 32;
+		float v[P];
 #pragma unroll
-			for (int j = 0; j < 8; j++) { c[j] = S.hist[lane * 8 + j]; run += c[j]; }
-			unsigned inc = run;
+		for (int j = 0; j < P; j++) v[j] = S.tmin[lane * P + j];
+		float kth = __int_as_float(0x7f800000);
+		for (int k = 0; k < K; k++) {
+			float m = v[0];
+			int mj = 0;
 #pragma unroll
-			for (int o = 1; o < 32; o <<= 1) {
-				const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
-				if (lane >= o) inc += v;
-			}
-			const unsigned excl = inc - run, rank = S.rank;
-			const unsigned ball = __ballot_sync(0xffffffffu, inc >= rank);
-			const int first = __ffs(ball) - 1;
-			if (lane == first) {
-				unsigned cum = excl;
-				int b = 0;
-				while (cum + c[b] < rank) { cum += c[b]; b++; }
-				S.prefix = pre | ((unsigned)(lane * 8 + b) << shift);
-				S.rank = rank - cum;
-				S.count_eq = c[b];
+			for (int j = 1; j < P; j++)
+				if (v[j] < m) { m = v[j]; mj = j; }
+			float w = m;
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) w = fminf(w, __shfl_xor_sync(0xffffffffu, w, o));
+			kth = w;
+			// remove one occurrence of the minimum (lowest lane holding it)
+			const unsigned holder = __ballot_sync(0xffffffffu, m == w);
+			if (lane == __ffs(holder) - 1) {
+#pragma unroll
+				for (int j = 0; j < P; j++)
+					if (j == mj) v[j] = __int_as_float(0x7f800000);
 			}
 		}
-		__syncthreads();
+		if (lane == 0) S.bound = kth;
 	}
-	// unique boundary: exactly K distances are <= the k-th one
-	const unsigned T = S.prefix;
-	const bool unique = S.count_eq == S.rank;
-	if (unique) {
-		for (int i = tid; i < ncand; i += blockDim.x)
-			if (__float_as_uint(dist[i]) <= T) {
-				const unsigned s = atomicAdd(&S.nsel, 1u);
-				if (s < (unsigned)kMaxNp) { S.sd[s] = dist[i]; S.si[s] = i; }
-			}
+	__syncthreads();
+	const float bound = S.bound;
+	for (int i = tid; i < ncand; i += blockDim.x) {
+		const float d = dist[i];
+		if (d <= bound) {
+			const unsigned s = atomicAdd(&S.nsel, 1u);
+			if (s < (unsigned)kSelCap) { S.sd[s] = d; S.si[s] = i; }
+		}
 	}
 	__syncthreads();
 	if (warp == 0) {
-		bool ok = unique && S.nsel == (unsigned)K;
+		const int n = (int)S.nsel;
+		bool ok = n >= K && n <= kSelCap;
 		if (ok) {
-			// bitonic sort of K <= 32 (distance, candidate) pairs across the warp
-			float d = lane < K ? S.sd[lane] : __int_as_float(0x7f800000);
-			int ix = lane < K ? S.si[lane] : 0x7fffffff;
-			for (int k = 2; k <= 32; k <<= 1)
+			// bitonic sort of up to 64 (distance, candidate) pairs, 2 per lane
+			float d0 = lane < n ? S.sd[lane] : __int_as_float(0x7f800000);
+			int i0 = lane < n ? S.si[lane] : 0x7fffffff;
+			float d1 = lane + 32 < n ? S.sd[lane + 32] : __int_as_float(0x7f800000);
+			int i1 = lane + 32 < n ? S.si[lane + 32] : 0x7fffffff;
+			// element e = lane + 32*h; compare-exchange across e ^ j
+			for (int k = 2; k <= 64; k <<= 1)
 				for (int j = k >> 1; j > 0; j >>= 1) {
-					const float od = __shfl_xor_sync(0xffffffffu, d, j);
-					const int oi = __shfl_xor_sync(0xffffffffu, ix, j);
-					const bool up = (lane & k) == 0, low = (lane & j) == 0;
-					const bool take = (low == up) ? (od < d || (od == d && oi < ix)) : (od > d || (od == d && oi > ix));
-					if (take) { d = od; ix = oi; }
+					if (j == 32) {
+						const bool up = (lane & k) == 0;   // k == 64 here: always ascending
+						const bool sw = up ? (d0 > d1 || (d0 == d1 && i0 > i1)) : (d0 < d1 || (d0 == d1 && i0 < i1));
+						if (sw) { float td = d0; d0 = d1; d1 = td; int ti = i0; i0 = i1; i1 = ti; }
+					} else {
+						const float od0 = __shfl_xor_sync(0xffffffffu, d0, j), od1 = __shfl_xor_sync(0xffffffffu, d1, j);
+						const int oi0 = __shfl_xor_sync(0xffffffffu, i0, j), oi1 = __shfl_xor_sync(0xffffffffu, i1, j);
+						const bool low = (lane & j) == 0;
+						const bool up0 = (lane & k) == 0, up1 = ((lane + 32) & k) == 0;
+						const bool t0 = (low == up0) ? (od0 < d0 || (od0 == d0 && oi0 < i0)) : (od0 > d0 || (od0 == d0 && oi0 > i0));
+						const bool t1 = (low == up1) ? (od1 < d1 || (od1 == d1 && oi1 < i1)) : (od1 > d1 || (od1 == d1 && oi1 > i1));
+						if (t0) { d0 = od0; i0 = oi0; }
+						if (t1) { d1 = od1; i1 = oi1; }
+					}
 				}
-			const float nd = __shfl_down_sync(0xffffffffu, d, 1);
-			const bool tie = lane + 1 < K && nd == d;
-			ok = __ballot_sync(0xffffffffu, tie) == 0u;
-			if (ok && lane < K) { S.sd[lane] = d; S.si[lane] = ix; }
+			// checks on the sorted list e = 0..n-1: distinct among the first K,
+			// and the K-th strictly below the (K+1)-th
+			const float nd0 = __shfl_down_sync(0xffffffffu, d0, 1);
+			const float first1 = __shfl_sync(0xffffffffu, d1, 0);
+			const float nxt0 = lane == 31 ? first1 : nd0;           // element lane+1
+			const float nd1 = __shfl_down_sync(0xffffffffu, d1, 1);  // element lane+33
+			const bool bad0 = lane + 1 < n && lane < K && nxt0 == d0;
+			const bool bad1 = lane + 33 < n && lane + 32 < K && nd1 == d1;
+			ok = __ballot_sync(0xffffffffu, bad0 || bad1) == 0u;
+			if (ok) {
+				if (lane < K) { S.sd[lane] = d0; S.si[lane] = i0; }
+				if (lane + 32 < K) { S.sd[lane + 32] = d1; S.si[lane + 32] = i1; }
+			}
 		}
 		if (!ok) {
 			// exact replay of libstdc++'s heap selection, candidates in order
@@ -423,129 +444,69 @@ __device__ void select_knn(const float *dist, int ncand, int K, SelectShared &S)
 	__syncthreads();
 }
 
-// One CTA handles one group at a time.  STAGE: every frame window of the group
-// is requested by TMA at once (one buffer and one mbarrier per frame); the
-// next group's windows are requested right after the distances are done, so
-// the loads overlap the k-nearest selection.
-template <int PX, int PT, bool REFREG, bool STAGE>
+// One CTA handles one group at a time: every thread computes register-tiled
+// strips of kSW candidates (window rows read through L1 from the video), then
+// the CTA selects the k nearest.  Several CTAs share an SM so that one CTA's
+// selection overlaps the others' distance work.
+template <int PX, int PT, bool REFREG>
 __global__ void __launch_bounds__(kThreads)
-search_kernel(const __grid_constant__ CUtensorMap map, Image src, StepParams sp, SearchArgs a)
+search_kernel(Image src, StepParams sp, SearchArgs a)
 {
-	extern __shared__ __align__(128) unsigned char smem_raw[];
-	const int box = a.BX * a.BY * a.CB * sp.pt;               // floats per window buffer
-	const int boxp = (box + 31) / 32 * 32;
-	float *wins = reinterpret_cast<float *>(smem_raw);
-	float *dist = wins + (STAGE ? (size_t)boxp * a.nfm : 0);
+	extern __shared__ __align__(16) float smem_f[];
+	float *dist = smem_f;
 	const int ncand_max = sp.wx * sp.wx * a.nfm;
 	float *ref_s = dist + ncand_max;                            // chn * spc
-	__shared__ FrameWin fw[2][kMaxFrames];
-	__shared__ int s_nframes[2], s_ncand[2], s_nitems[2], s_tile[2], s_x[2], s_y[2], s_t[2];
-	__shared__ __align__(8) uint64_t bars[kMaxFrames];
-	__shared__ unsigned s_phase[kMaxFrames];
-	__shared__ int s_abort;
+	__shared__ FrameWin fw[kMaxFrames];
+	__shared__ int s_nframes, s_ncand, s_nitems, s_tile, s_x, s_y, s_t;
 	__shared__ SelectShared S;
 
 	const int tid = threadIdx.x;
 	const int chn = sp.chn_search;
-	const unsigned box_bytes = (unsigned)box * 4u;
-
-	auto request = [&](int slot) {
-		// thread 0: TMA loads of every frame window of the group planned in slot
-		const Tile T = a.tiles[s_tile[slot]];
-		for (int ii = 0; ii < s_nframes[slot]; ii++) {
-			const FrameWin &f = fw[slot][ii];
-			mbar_expect_tx(&bars[ii], box_bytes);
-			tma_load_4d(wins + (size_t)ii * boxp, &map, &bars[ii], f.X0, T.oy + f.ry0, 0, f.qt);
-			s_phase[ii]++;
-		}
-	};
-
-	int cur = 0;
-	long long g = a.g_begin + blockIdx.x;
-	if (tid == 0) {
-		s_abort = 0;
-		for (int ii = 0; ii < kMaxFrames; ii++) s_phase[ii] = 0u;
-		if (STAGE) {
-			for (int ii = 0; ii < a.nfm; ii++) mbar_init(&bars[ii], 1);
-			asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-		}
-		if (g < a.g_end) {
-			plan_group(a, sp, g, fw[0], s_nframes[0], s_ncand[0], s_nitems[0], s_tile[0], s_x[0], s_y[0], s_t[0], 0);
-			if (STAGE) request(0);
-		}
-	}
-	__syncthreads();
-
-	for (; g < a.g_end; g += gridDim.x) {
-		const Tile T = a.tiles[s_tile[cur]];
-		const int nframes = s_nframes[cur];
+	for (long long g = a.g_begin + blockIdx.x; g < a.g_end; g += gridDim.x) {
+		if (tid == 0)
+			plan_group(a, sp, g, fw, s_nframes, s_ncand, s_nitems, s_tile, s_x, s_y, s_t, 0);
+		__syncthreads();
+		const Tile T = a.tiles[s_tile];
+		const int nframes = s_nframes;
 		float ref_r[(PX > 0 ? PX * PX * PT : 1)];
 		if (REFREG) {
 #pragma unroll
 			for (int k = 0; k < (PX > 0 ? PX * PX * PT : 1); k++) {
 				constexpr int Q = PX > 0 ? PX : 1;
 				const int ht = k / (Q * Q), hy = (k / Q) % Q, hx = k % Q;
-				ref_r[k] = __ldg(src.p + src.at(T.ox + s_x[cur] + hx, T.oy + s_y[cur] + hy, s_t[cur] + ht, 0));
+				ref_r[k] = __ldg(src.p + src.at(T.ox + s_x + hx, T.oy + s_y + hy, s_t + ht, 0));
 			}
 		} else {
 			for (int k = tid; k < sp.spc * chn; k += blockDim.x) {
 				const int c = k / sp.spc, r = k % sp.spc;
 				const int ht = r / (sp.px * sp.px), hy = (r / sp.px) % sp.px, hx = r % sp.px;
-				ref_s[k] = src.p[src.at(T.ox + s_x[cur] + hx, T.oy + s_y[cur] + hy, s_t[cur] + ht, c)];
+				ref_s[k] = src.p[src.at(T.ox + s_x + hx, T.oy + s_y + hy, s_t + ht, c)];
 			}
 			__syncthreads();
 		}
-
 		// distances of every candidate, stored in the reference's candidate order
-		const int nit = s_nitems[cur];
+		const int nit = s_nitems;
+		float tmin = __int_as_float(0x7f800000);
 		int ii = 0;
 		for (int it = tid; it < nit; it += blockDim.x) {
-			while (ii + 1 < nframes && fw[cur][ii + 1].ibase <= it) ii++;
-			const FrameWin f = fw[cur][ii];
-			if (STAGE) {
-				// bounded wait for this frame's window
-				const unsigned parity = (s_phase[ii] - 1u) & 1u;
-				unsigned n = 0;
-				while (!mbar_try_wait(&bars[ii], parity))
-					if (++n > kWaitLimit) { s_abort = 1; atomicExch(a.err, 1); break; }
-				if (s_abort) break;
-			}
+			while (ii + 1 < nframes && fw[ii + 1].ibase <= it) ii++;
+			const FrameWin f = fw[ii];
 			const int nstrip = (f.nx + kSW - 1) / kSW;
 			const int rel = it - f.ibase;
 			const int row = rel / nstrip, strip = rel - row * nstrip;
 			float acc[kSW];
-			if (STAGE) {
-				const float *base = wins + (size_t)ii * boxp + (size_t)row * a.BX;
-				strip_distances<PX, PT, REFREG>(base, a.BX, (size_t)a.BX * a.BY, (size_t)a.BX * a.BY * a.CB,
-				                                f.xoff + strip * kSW, a.BX - 1, chn, sp.px, sp.pt, ref_s, ref_r, acc);
-			} else {
-				const float *base = src.p + src.at(0, T.oy + f.ry0 + row, f.qt, 0);
-				strip_distances<PX, PT, REFREG>(base, src.P, src.plane(), src.plane() * src.C,
-				                                T.ox + f.rx0 + strip * kSW, T.ox + T.w - 1, chn, sp.px, sp.pt,
-				                                ref_s, ref_r, acc);
-			}
+			const float *base = src.p + src.at(0, T.oy + f.ry0 + row, f.qt, 0);
+			strip_distances<PX, PT, REFREG>(base, src.P, src.plane(), src.plane() * src.C, T.ox + f.rx0 + strip * kSW,
+			                                T.ox + T.w - 1, chn, sp.px, sp.pt, ref_s, ref_r, acc);
 			float *dd = dist + f.cbase + row * f.nx + strip * kSW;
 #pragma unroll
 			for (int j = 0; j < kSW; j++)
-				if (strip * kSW + j < f.nx) dd[j] = acc[j];
+				if (strip * kSW + j < f.nx) { dd[j] = acc[j]; tmin = fminf(tmin, acc[j]); }
 		}
 		__syncthreads();
-		if (s_abort) return;
-
-		// plan the next group and request its windows: they load during the selection
-		if (tid == 0 && g + gridDim.x < a.g_end) {
-			const int sl = cur ^ 1;
-			plan_group(a, sp, g + gridDim.x, fw[sl], s_nframes[sl], s_ncand[sl], s_nitems[sl], s_tile[sl], s_x[sl],
-			           s_y[sl], s_t[sl], 0);
-			if (STAGE) {
-				asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-				request(sl);
-			}
-		}
-
-		const int ncand = s_ncand[cur];
+		const int ncand = s_ncand;
 		const int K = min(sp.np, ncand);
-		select_knn(dist, ncand, K, S);
+		select_knn(dist, ncand, K, tmin, S);
 		if (tid == 0) {
 			int n = 1;
 			while (2 * n <= K && S.sd[n] < sp.tau2) n *= 2;   // nldct.cpp:1284-1289
@@ -553,17 +514,15 @@ search_kernel(const __grid_constant__ CUtensorMap map, Image src, StepParams sp,
 			for (int q = 0; q < n; q++) {
 				const int c = S.si[q];
 				int jj = 0;
-				while (jj + 1 < nframes && fw[cur][jj + 1].cbase <= c) jj++;
-				const FrameWin &f = fw[cur][jj];
+				while (jj + 1 < nframes && fw[jj + 1].cbase <= c) jj++;
+				const FrameWin &f = fw[jj];
 				const int rl = c - f.cbase;
 				const int qy = f.ry0 + rl / f.nx, qx = f.rx0 + rl % f.nx;
 				a.idx[g * sp.np + q] = (uint32_t)(((long long)f.qt * T.h + qy) * T.w + qx);
 			}
 		}
 		__syncthreads();
-		cur ^= 1;
 	}
-	// every window requested belongs to a group of this CTA and was waited for
 }
 
 // nSimilarPatches == 1: the group is the reference patch alone (nldct.cpp:1326-1327).
@@ -595,19 +554,19 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 	return fn;
 }
 
-template <int PX, int PT, bool REFREG, bool STAGE>
-cudaError_t launch_t(const CUtensorMap &map, const Image &src, const StepParams &sp, const SearchArgs &a,
-                     size_t smem, int nsm, long long n, cudaStream_t st)
+template <int PX, int PT, bool REFREG>
+cudaError_t launch_t(const Image &src, const StepParams &sp, const SearchArgs &a, size_t smem, int nsm,
+                     long long n, cudaStream_t st)
 {
-	cudaError_t e = cudaFuncSetAttribute(search_kernel<PX, PT, REFREG, STAGE>,
-	                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaError_t e = cudaFuncSetAttribute(search_kernel<PX, PT, REFREG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                     (int)smem);
 	if (e != cudaSuccess) return e;
 	int per_sm = 0;
-	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, search_kernel<PX, PT, REFREG, STAGE>, kThreads, smem);
+	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, search_kernel<PX, PT, REFREG>, kThreads, smem);
 	if (e != cudaSuccess) return e;
 	long long blocks = (long long)nsm * (per_sm < 1 ? 1 : per_sm);
 	if (blocks > n) blocks = n;
-	search_kernel<PX, PT, REFREG, STAGE><<<(int)blocks, kThreads, smem, st>>>(map, src, sp, a);
+	search_kernel<PX, PT, REFREG><<<(int)blocks, kThreads, smem, st>>>(src, sp, a);
 	return cudaGetLastError();
 }
 
@@ -651,43 +610,14 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
 	a.idx = idx;
 	a.err = err;
 	const long long n = g_end - g_begin;
-	const int box = a.BX * a.BY * a.CB * sp.pt;
-	const size_t boxp = (size_t)(box + 31) / 32 * 32;
 	const size_t ncand = (size_t)sp.wx * sp.wx * a.nfm;
-	const size_t small = sizeof(float) * (ncand + (size_t)sp.spc * sp.chn_search);
-	const size_t staged = small + sizeof(float) * boxp * a.nfm;
-	const bool stage = a.BX <= 256 && a.BY <= 256 && sp.pt <= 256 && staged <= 110 * 1024;
-
-	CUtensorMap map;
-	std::memset(&map, 0, sizeof(map));
-	if (stage) {
-		PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
-		if (!enc) return cudaErrorNotSupported;
-		const cuuint64_t dims[4] = {(cuuint64_t)src.P, (cuuint64_t)src.H, (cuuint64_t)src.C, (cuuint64_t)src.F};
-		const cuuint64_t strides[3] = {(cuuint64_t)src.P * 4, (cuuint64_t)src.P * src.H * 4,
-		                               (cuuint64_t)src.P * src.H * src.C * 4};
-		const cuuint32_t boxd[4] = {(cuuint32_t)a.BX, (cuuint32_t)a.BY, (cuuint32_t)a.CB, (cuuint32_t)sp.pt};
-		const cuuint32_t estr[4] = {1, 1, 1, 1};
-		CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src.p, dims, strides, boxd, estr,
-		                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-		                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-		if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
-	}
-	const size_t smem = stage ? staged : small;
+	const size_t smem = sizeof(float) * (ncand + (size_t)sp.spc * sp.chn_search);
 	const bool one = sp.chn_search == 1;
-	if (sp.px == 4 && sp.pt == 4) {
-		if (one && stage) return launch_t<4, 4, true, true>(map, src, sp, a, smem, nsm, n, st);
-		if (one) return launch_t<4, 4, true, false>(map, src, sp, a, smem, nsm, n, st);
-		if (stage) return launch_t<4, 4, false, true>(map, src, sp, a, smem, nsm, n, st);
-		return launch_t<4, 4, false, false>(map, src, sp, a, smem, nsm, n, st);
-	}
-	if (sp.px == 8 && sp.pt == 1) {
-		if (one && stage) return launch_t<8, 1, true, true>(map, src, sp, a, smem, nsm, n, st);
-		if (stage) return launch_t<8, 1, false, true>(map, src, sp, a, smem, nsm, n, st);
-		return launch_t<8, 1, false, false>(map, src, sp, a, smem, nsm, n, st);
-	}
-	if (stage) return launch_t<0, 0, false, true>(map, src, sp, a, smem, nsm, n, st);
-	return launch_t<0, 0, false, false>(map, src, sp, a, smem, nsm, n, st);
+	if (sp.px == 4 && sp.pt == 4)
+		return one ? launch_t<4, 4, true>(src, sp, a, smem, nsm, n, st) : launch_t<4, 4, false>(src, sp, a, smem, nsm, n, st);
+	if (sp.px == 8 && sp.pt == 1)
+		return one ? launch_t<8, 1, true>(src, sp, a, smem, nsm, n, st) : launch_t<8, 1, false>(src, sp, a, smem, nsm, n, st);
+	return launch_t<0, 0, false>(src, sp, a, smem, nsm, n, st);
 }
 
 }  // namespace bm4dof
