@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 
 #include "common.cuh"
@@ -38,8 +39,9 @@ namespace bm4dof {
 
 namespace {
 
-constexpr int kThreads = 128;
-constexpr int kSW = 7;                 // candidates per thread along x
+constexpr int kThreads = 192;          // 6 warps: 567 column strips of a 21x21x9 window set in 3 rounds
+constexpr int kSW = 7;                 // candidates per thread along x (horizontal strips)
+constexpr int kR = 7;                  // candidates per thread along y (column strips)
 constexpr unsigned kWaitLimit = 1u << 24;
 
 struct FrameWin {
@@ -236,7 +238,7 @@ __device__ void plan_group(const SearchArgs &a, const StepParams &sp, long long 
 		f.X0 = (T.ox + rx0) & ~3;           // TMA x coordinate: 16-byte aligned
 		f.xoff = T.ox + rx0 - f.X0;
 		cb += f.nx * f.ny;
-		ib += f.ny * ((f.nx + kSW - 1) / kSW);
+		ib += f.nx * ((f.ny + kR - 1) / kR);
 		fw[ii] = f;
 	}
 	nframes = nwt;
@@ -444,6 +446,64 @@ __device__ void select_knn(const float *dist, int ncand, int K, float tmin, Sele
 	__syncthreads();
 }
 
+// Distances of kR vertically adjacent candidates (one column of the window,
+// rows r = 0..kR-1 below `col`, which points at candidate row 0, patch frame
+// 0, channel 0).  Each image row is loaded once and feeds every candidate
+// whose patch covers it; per candidate the terms still follow the reference's
+// (c, ht, hy, hx) order.  Consecutive lanes take consecutive columns, so each
+// warp-wide load touches one or two contiguous row segments.
+template <int PX, int PT, bool REFREG>
+__device__ __forceinline__ void col_distances(const float *col, size_t rpitch, size_t cpitch, size_t tpitch,
+                                              int ymax, int chn, int px_rt, int pt_rt, const float *ref_s,
+                                              const float (&ref_r)[(PX > 0 ? PX * PX * PT : 1)], float acc[kR])
+{
+#pragma unroll
+	for (int r = 0; r < kR; r++) acc[r] = 0.f;
+	if (PX > 0) {
+		constexpr int SPC = (PX > 0 ? PX * PX * PT : 1);
+		constexpr int Q = PX > 0 ? PX : 1;
+		for (int c = 0; c < chn; c++)
+#pragma unroll
+			for (int ht = 0; ht < (PT > 0 ? PT : 1); ht++)
+#pragma unroll
+				for (int yy = 0; yy < kR + Q - 1; yy++) {
+					const float *row = col + ht * tpitch + c * cpitch + (size_t)min(yy, ymax) * rpitch;
+					float v[Q];
+#pragma unroll
+					for (int hx = 0; hx < Q; hx++) v[hx] = __ldg(row + hx);
+#pragma unroll
+					for (int r = 0; r < kR; r++) {
+						const int hy = yy - r;
+						if (hy >= 0 && hy < Q) {
+#pragma unroll
+							for (int hx = 0; hx < Q; hx++) {
+								const int kk = (ht * Q + hy) * Q + hx;
+								const float rv = REFREG ? ref_r[kk] : ref_s[c * SPC + kk];
+								const float d = __fsub_rn(rv, v[hx]);
+								acc[r] = __fadd_rn(acc[r], __fmul_rn(d, d));
+							}
+						}
+					}
+				}
+	} else {
+		const int px = px_rt, pt = pt_rt, spc = px * px * pt;
+		for (int c = 0; c < chn; c++)
+			for (int ht = 0; ht < pt; ht++)
+				for (int yy = 0; yy < kR + px - 1; yy++) {
+					const float *row = col + ht * tpitch + c * cpitch + (size_t)min(yy, ymax) * rpitch;
+#pragma unroll
+					for (int r = 0; r < kR; r++) {
+						const int hy = yy - r;
+						if (hy < 0 || hy >= px) continue;
+						for (int hx = 0; hx < px; hx++) {
+							const float d = __fsub_rn(ref_s[c * spc + (ht * px + hy) * px + hx], __ldg(row + hx));
+							acc[r] = __fadd_rn(acc[r], __fmul_rn(d, d));
+						}
+					}
+				}
+	}
+}
+
 // One CTA handles one group at a time: every thread computes register-tiled
 // strips of kSW candidates (window rows read through L1 from the video), then
 // the CTA selects the k nearest.  Several CTAs share an SM so that one CTA's
@@ -491,17 +551,17 @@ search_kernel(Image src, StepParams sp, SearchArgs a)
 		for (int it = tid; it < nit; it += blockDim.x) {
 			while (ii + 1 < nframes && fw[ii + 1].ibase <= it) ii++;
 			const FrameWin f = fw[ii];
-			const int nstrip = (f.nx + kSW - 1) / kSW;
 			const int rel = it - f.ibase;
-			const int row = rel / nstrip, strip = rel - row * nstrip;
-			float acc[kSW];
-			const float *base = src.p + src.at(0, T.oy + f.ry0 + row, f.qt, 0);
-			strip_distances<PX, PT, REFREG>(base, src.P, src.plane(), src.plane() * src.C, T.ox + f.rx0 + strip * kSW,
-			                                T.ox + T.w - 1, chn, sp.px, sp.pt, ref_s, ref_r, acc);
-			float *dd = dist + f.cbase + row * f.nx + strip * kSW;
+			const int rb = rel / f.nx, cx = rel - rb * f.nx;   // row block, column
+			const int qy0 = rb * kR;
+			float acc[kR];
+			const float *colp = src.p + src.at(T.ox + f.rx0 + cx, T.oy + f.ry0 + qy0, f.qt, 0);
+			col_distances<PX, PT, REFREG>(colp, src.P, src.plane(), src.plane() * src.C, f.ny - qy0 + sp.px - 2,
+			                              chn, sp.px, sp.pt, ref_s, ref_r, acc);
+			float *dd = dist + f.cbase + qy0 * f.nx + cx;
 #pragma unroll
-			for (int j = 0; j < kSW; j++)
-				if (strip * kSW + j < f.nx) { dd[j] = acc[j]; tmin = fminf(tmin, acc[j]); }
+			for (int r = 0; r < kR; r++)
+				if (qy0 + r < f.ny) { dd[r * f.nx] = acc[r]; tmin = fminf(tmin, acc[r]); }
 		}
 		__syncthreads();
 		const int ncand = s_ncand;
@@ -612,7 +672,14 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
 	const long long n = g_end - g_begin;
 	const size_t ncand = (size_t)sp.wx * sp.wx * a.nfm;
 	const size_t smem = sizeof(float) * (ncand + (size_t)sp.spc * sp.chn_search);
-	const bool one = sp.chn_search == 1;
+	// one searched channel: the reference patch may live in registers
+	// (BM4DOF_SEARCH_REFREG=0 keeps it in shared memory: fewer registers,
+	// more resident CTAs)
+	static const int refreg_env = [] {
+		const char *e = std::getenv("BM4DOF_SEARCH_REFREG");
+		return e ? std::atoi(e) : 1;
+	}();
+	const bool one = sp.chn_search == 1 && refreg_env != 0;
 	if (sp.px == 4 && sp.pt == 4)
 		return one ? launch_t<4, 4, true>(src, sp, a, smem, nsm, n, st) : launch_t<4, 4, false>(src, sp, a, smem, nsm, n, st);
 	if (sp.px == 8 && sp.pt == 1)
