@@ -672,12 +672,13 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
 	const long long n = g_end - g_begin;
 	const size_t ncand = (size_t)sp.wx * sp.wx * a.nfm;
 	const size_t smem = sizeof(float) * (ncand + (size_t)sp.spc * sp.chn_search);
-	// one searched channel: the reference patch may live in registers
-	// (BM4DOF_SEARCH_REFREG=0 keeps it in shared memory: fewer registers,
-	// more resident CTAs)
+	// The reference patch in shared memory (80 registers, four CTAs per SM)
+	// measured faster than in registers (168 registers, two CTAs per SM):
+	// 179 vs 231 ms on 854x480x20.  BM4DOF_SEARCH_REFREG=1 selects the
+	// register variant.
 	static const int refreg_env = [] {
 		const char *e = std::getenv("BM4DOF_SEARCH_REFREG");
-		return e ? std::atoi(e) : 1;
+		return e ? std::atoi(e) : 0;
 	}();
 	const bool one = sp.chn_search == 1 && refreg_env != 0;
 	if (sp.px == 4 && sp.pt == 4)
