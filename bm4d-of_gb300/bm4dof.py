@@ -38,7 +38,7 @@ EXPORTS = [
     "bm4dof_initialize_params", "bm4dof_set_size_search_window", "bm4dof_set_size_patch",
     "bm4dof_set_n_similar_patches", "bm4dof_format_params", "bm4dof_print_params",
     "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run",
-    "bm4dof_get_groups", "bm4dof_last_timings",
+    "bm4dof_get_groups", "bm4dof_last_timings", "bm4dof_search_groups_noalloc",
 ]
 
 
@@ -112,6 +112,10 @@ def load(path: str = LIB_PATH):
     L.bm4dof_get_groups.restype = C.c_int
     L.bm4dof_last_timings.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint)]
     L.bm4dof_last_timings.restype = C.c_int
+    L.bm4dof_search_groups_noalloc.argtypes = [C.c_void_p] * 3 + [C.c_uint] * 4 + [
+        C.POINTER(Params), C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint, C.c_size_t,
+        C.POINTER(C.c_size_t), C.c_void_p]
+    L.bm4dof_search_groups_noalloc.restype = C.c_int
     _lib = L
     return L
 

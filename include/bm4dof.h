@@ -156,6 +156,28 @@ bm4dof_status bm4dof_get_groups(bm4dof_ctx *ctx, unsigned step, unsigned tile,
                                 unsigned *ref, unsigned *nsimp, unsigned *index,
                                 unsigned stride, size_t cap, size_t *count);
 
+/* Patch search of one tile with no device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc (code inside
+ * another framework's memory pool, plug-in hosts that own every device
+ * buffer, pipelines that forbid allocation once running).  The caller passes
+ * device pointers for the video to search (the noisy video for step 1, the
+ * basic estimate for step 2; already colour transformed when C > 1), the
+ * flows (both or neither) and the outputs; all working memory is one static
+ * device array of 32 MiB per device, held for the life of the process.
+ * Returns BM4DOF_ERR_ARGUMENT with the needed size when a tile does not fit.
+ * Outputs, in processing order, for every grid group of tile `tile` of
+ * `nparts` tiles: ref[g], nsimp[g] and index[g*stride + n] in the format of
+ * bm4dof_get_groups (at most cap groups are written; *count = total).  The
+ * mask switch-offs of bm4dof_run are not applied.  The first call on a device
+ * looks up the scratch's device address, so make it before any stream
+ * capture.  Asynchronous on `stream` (a cudaStream_t, NULL for the default
+ * stream); calls that overlap on the GPU share the scratch and race. */
+bm4dof_status bm4dof_search_groups_noalloc(const float *video, const float *fflow, const float *bflow,
+                                           unsigned width, unsigned height, unsigned channels, unsigned frames,
+                                           const bm4dof_params *params, unsigned nparts, unsigned tile,
+                                           unsigned *ref, unsigned *nsimp, unsigned *index, unsigned stride,
+                                           size_t cap, size_t *count, void *stream);
+
 /* Device times (milliseconds, CUDA events on the context's stream) of the
  * last bm4dof_run: ms[0] patch search, ms[1] group filter, ms[2] aggregation,
  * ms[3] everything else (copies, colour, normalisation), ms[4] the whole call
