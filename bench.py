@@ -286,6 +286,23 @@ def main():
         "quality_db": {"noisy": psnr(nz, clean), "final": psnr(final_np, clean)},
         "wall_s_timed": wall,
     }
+    # the faster forms of the same workload, timed the same way, with their
+    # PSNR loss against the plain method
+    forms = {}
+    for name, kw in (("mixed", {"mixed": True}),):
+        for _ in range(2):
+            ctx.runNlBayes(d_nz, d_ff, d_bf, p1, p2, basic=d_basic, final=d_final, nparts=args.nparts, **kw)
+        tms = []
+        for _ in range(args.steps):
+            ctx.runNlBayes(d_nz, d_ff, d_bf, p1, p2, basic=d_basic, final=d_final, nparts=args.nparts, **kw)
+            ms, _ = ctx.timings()
+            tms.append(ms[4])
+        fq = psnr(d_final.cpu().numpy(), clean)
+        forms[name] = {"value": world * mpf / (statistics.mean(tms) / 1e3), "unit": UNIT,
+                       "ms_per_step": statistics.mean(tms), "stage_ms": dict(zip(
+                           ("search", "filter", "aggregation", "other", "total"), ctx.timings()[0])),
+                       "psnr_db": fq, "psnr_loss_vs_plain_db": line["quality_db"]["final"] - fq}
+    line["forms"] = forms
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(nz, ff, bf, sigma)
     print(json.dumps(line), flush=True)

@@ -23,7 +23,8 @@ LIB = os.path.join(OUT, "libbm4dof_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
-SOURCES = ["search.cu", "filter.cu", "aggregate.cu", "runtime.cu", "noalloc.cu", "params.cpp", "basis.cpp"]
+SOURCES = ["search.cu", "search_mixed.cu", "filter.cu", "aggregate.cu", "runtime.cu", "noalloc.cu",
+           "params.cpp", "basis.cpp"]
 
 
 def nvcc() -> str:

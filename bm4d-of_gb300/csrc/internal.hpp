@@ -30,6 +30,13 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
                           const uint32_t *traj, const StepParams &sp, long long g_begin, long long g_end,
                           uint8_t *nsimp, uint32_t *idx, int *err, int nsm, cudaStream_t st);
 
+// search_mixed.cu
+void mixed_blocks(const std::vector<Tile> &tiles, std::vector<long long> &out);
+bool mixed_supported(const StepParams &sp);
+cudaError_t launch_search_mixed(const Image &src, const Tile *tiles, int ntiles, const int *grid,
+                                const uint32_t *traj, const StepParams &sp, const long long *blocks,
+                                long long nblocks, uint8_t *nsimp, uint32_t *idx, int nsm, cudaStream_t st);
+
 // filter.cu
 size_t filter_smem_bytes(const StepParams &sp);
 cudaError_t launch_filter(const Image &noisy, const Image &basic, const Tile *tiles, int ntiles,

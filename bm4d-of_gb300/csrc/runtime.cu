@@ -243,12 +243,16 @@ bm4dof_status check_params(const bm4dof_params &p)
 	return BM4DOF_OK;
 }
 
+struct RunMode {
+	bool mixed = false;   // FP16 pre-screen search (+ BF16 transforms where built)
+};
+
 // One step of processNlBayes over all tiles.  out receives the rebuilt video
 // (inverse colour transformed when inverse_color).
 bm4dof_status run_step(bm4dof_ctx *ctx, int step, const bm4dof_params &p, const Image &noisy,
                        const Image &basic, const Image &ffl, const Image &bfl, bool use_flow,
                        unsigned nparts, const Image &out, bool inverse_color, bool keep,
-                       float *ratio)
+                       float *ratio, const RunMode &mode)
 {
 	const unsigned W = noisy.W, H = noisy.H, C = noisy.C, F = noisy.F;
 	cudaStream_t st = ctx->st;
@@ -317,8 +321,19 @@ bm4dof_status run_step(bm4dof_ctx *ctx, int step, const bm4dof_params &p, const 
 	{
 		Mark m(ctx, T_SEARCH);
 		CK(launch_traj(ffl, bfl, d_tiles, ntiles, d_grid, sp, G, d_traj, st));
-		CK(launch_search(step == 1 ? noisy : basic, d_tiles, ntiles, d_grid, d_traj, sp, 0, G, d_nsimp, d_idx,
-		                 reinterpret_cast<int *>(d_small + 2), ctx->nsm, st));
+		if (mode.mixed && mixed_supported(sp)) {
+			// FP16 tensor-core pre-screen + exact re-rank of the best 2k
+			std::vector<long long> blocks;
+			mixed_blocks(pl.tiles, blocks);
+			long long *d_blocks;
+			DBUF("mixed_blocks", blocks.size(), d_blocks);
+			CK(cudaMemcpyAsync(d_blocks, blocks.data(), sizeof(long long) * blocks.size(), cudaMemcpyHostToDevice, st));
+			CK(launch_search_mixed(step == 1 ? noisy : basic, d_tiles, ntiles, d_grid, d_traj, sp, d_blocks,
+			                       (long long)blocks.size(), d_nsimp, d_idx, ctx->nsm, st));
+		} else {
+			CK(launch_search(step == 1 ? noisy : basic, d_tiles, ntiles, d_grid, d_traj, sp, 0, G, d_nsimp, d_idx,
+			                 reinterpret_cast<int *>(d_small + 2), ctx->nsm, st));
+		}
 		ctx->launches += 2;
 	}
 
@@ -553,7 +568,7 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
 		return BM4DOF_ERR_NO_STEP;
 	}
 	if (step != 1 && !final_) { set_error("bm4dof_run: final output is NULL"); return BM4DOF_ERR_ARGUMENT; }
-	if (flags & ~(BM4DOF_DEVICE_POINTERS | BM4DOF_KEEP_GROUPS)) {
+	if (flags & ~(BM4DOF_DEVICE_POINTERS | BM4DOF_KEEP_GROUPS | BM4DOF_MIXED_PRECISION)) {
 		set_error("bm4dof_run: unsupported flags");
 		return BM4DOF_ERR_UNSUPPORTED;
 	}
@@ -571,6 +586,8 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
 	ctx->kept[0].clear();
 	ctx->kept[1].clear();
 	const bool keep = (flags & BM4DOF_KEEP_GROUPS) != 0;
+	RunMode mode;
+	mode.mixed = (flags & BM4DOF_MIXED_PRECISION) != 0;
 	if (!ctx->t_begin) {
 		CK(cudaEventCreate(&ctx->t_begin));
 		CK(cudaEventCreate(&ctx->t_end));
@@ -615,7 +632,7 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
 	if (step != 2) {
 		const bool yuv = color && p1->colorSpace == BM4DOF_YUV;
 		bm4dof_status s = run_step(ctx, 1, *p1, yuv ? in_yuv : in, in, ff, bf, use_flow, nparts, bas,
-		                           yuv, keep, &gr[0]);
+		                           yuv, keep, &gr[0], mode);
 		if (s != BM4DOF_OK) return s;
 	}
 	if (step != 1) {
@@ -629,7 +646,7 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
 			ctx->launches++;
 		}
 		bm4dof_status s = run_step(ctx, 2, *p2, yuv ? in_yuv : in, bas_yuv, ff, bf, use_flow, nparts, fin,
-		                           yuv, keep, &gr[1]);
+		                           yuv, keep, &gr[1], mode);
 		if (s != BM4DOF_OK) return s;
 		if (yuv) {
 			// the reference returns basic after a forward and inverse transform (nldct.cpp:423, 467)
