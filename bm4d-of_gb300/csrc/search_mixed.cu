@@ -31,8 +31,8 @@ namespace {
 constexpr int kRefs = 16;           // reference patches per CTA (the MMA M)
 constexpr int kThreads = 128;       // 4 warps
 constexpr int kTop = 32;            // approximate candidates kept per reference (2k)
-constexpr int kCW = 64;             // candidate columns per chunk (multiple of 8)
-constexpr int kCH = 16;             // candidate rows per chunk
+constexpr int kCW = 96;             // candidate columns per chunk (multiple of 8): 16 windows at offset 3
+constexpr int kCH = 24;             // candidate rows per chunk: one window plus flow spread
 constexpr float kShift = 128.f;     // values are centred before the FP16 conversion
 
 struct RefWin {
@@ -128,13 +128,11 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 	static_assert(K == 64, "mixed search expects 64-element patches");
 	constexpr int WX = kCW + PX - 1, WY = kCH + PX - 1;
 	constexpr int WXP = (WX + 1 + 7) / 8 * 8;                   // FP16 row pitch (16-byte rows)
-	// dynamic shared memory: two FP16 copies of the chunk window ([shift][ht][y][x],
-	// copy 1 shifted one column left so every candidate column has an aligned
-	// pair), row sums of squares, |q'|^2, and the per-reference distances
+	// dynamic shared memory: the chunk window in centred FP16 ([ht][y][x]),
+	// |q'|^2 of every chunk candidate, and the per-reference distances
 	extern __shared__ __align__(16) unsigned char dsm[];
-	__half(*win16)[PT][WY][WXP] = reinterpret_cast<__half(*)[PT][WY][WXP]>(dsm);
-	float(*rowsq)[WY][kCW] = reinterpret_cast<float(*)[WY][kCW]>(dsm + sizeof(__half) * 2 * PT * WY * WXP);
-	float(*qn)[kCW] = reinterpret_cast<float(*)[kCW]>(reinterpret_cast<unsigned char *>(rowsq) + sizeof(float) * PT * WY * kCW);
+	__half(*win16)[WY][WXP] = reinterpret_cast<__half(*)[WY][WXP]>(dsm);
+	float(*qn)[kCW] = reinterpret_cast<float(*)[kCW]>(dsm + sizeof(__half) * PT * WY * WXP);
 	float *distb = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(qn) + sizeof(float) * kCH * kCW);
 	const int wmax = sp.wx * sp.wx;
 #define dist(r, i) distb[(r) * wmax + (i)]
@@ -240,38 +238,43 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 			for (int cy0 = uy0; cy0 <= uy1; cy0 += kCH)
 				for (int cx0 = ux0; cx0 <= ux1; cx0 += kCW) {
 					const int cw = min(kCW, ux1 - cx0 + 1), ch = min(kCH, uy1 - cy0 + 1);
-					// chunk pixels -> centred FP16 (two copies, the second shifted by
-					// one column so that every candidate column has an aligned pair),
-					// and row sums of squares
-					for (int i = tid; i < PT * (ch + PX - 1) * (cw + PX - 1); i += blockDim.x) {
-						const int ww = cw + PX - 1, hh = ch + PX - 1;
-						const int x = i % ww, y = (i / ww) % hh, ht = i / (ww * hh);
-						const float v = __ldg(src.p + src.at(T.ox + cx0 + x, T.oy + cy0 + y, qt + ht, 0)) - kShift;
-						const __half hv = __float2half_rn(v);
-						win16[0][ht][y][x] = hv;
-						if (x > 0) win16[1][ht][y][x - 1] = hv;
+					// chunk pixels -> centred FP16: one warp per row, lanes along x
+					const int ww = cw + PX - 1, hh = ch + PX - 1;
+					for (int row = warp; row < PT * hh; row += kThreads / 32) {
+						const int ht = row / hh, y = row - ht * hh;
+						const float *gp = src.p + src.at(T.ox + cx0, T.oy + cy0 + y, qt + ht, 0);
+						__half *dp = &win16[ht][y][0];
+						for (int x = lane; x < ww; x += 32) dp[x] = __float2half_rn(__ldg(gp + x) - kShift);
 					}
 					__syncthreads();
-					for (int i = tid; i < PT * (ch + PX - 1) * cw; i += blockDim.x) {
-						const int hh = ch + PX - 1;
-						const int x = i % cw, y = (i / cw) % hh, ht = i / (cw * hh);
-						float s = 0.f;
+					// |q'|^2 of every candidate from the rounded values: each thread
+					// slides a PX-row window down one candidate column
+					for (int x = tid; x < cw; x += kThreads) {
+						float col[kCH];
 #pragma unroll
-						for (int hx = 0; hx < PX; hx++) {
-							const float v = __half2float(win16[0][ht][y][x + hx]);
-							s = fmaf(v, v, s);
+						for (int y = 0; y < kCH; y++) col[y] = 0.f;
+#pragma unroll
+						for (int ht = 0; ht < PT; ht++) {
+							float rs[kCH + PX - 1];
+#pragma unroll
+							for (int y = 0; y < kCH + PX - 1; y++) {
+								float sq = 0.f;
+								if (y < hh)
+#pragma unroll
+									for (int hx = 0; hx < PX; hx++) {
+										const float v = __half2float(win16[ht][y][x + hx]);
+										sq = fmaf(v, v, sq);
+									}
+								rs[y] = sq;
+							}
+#pragma unroll
+							for (int y = 0; y < kCH; y++)
+#pragma unroll
+								for (int hy = 0; hy < PX; hy++) col[y] += rs[y + hy];
 						}
-						rowsq[ht][y][x] = s;
-					}
-					__syncthreads();
-					for (int i = tid; i < ch * cw; i += blockDim.x) {
-						const int x = i % cw, y = i / cw;
-						float s = 0.f;
 #pragma unroll
-						for (int ht = 0; ht < PT; ht++)
-#pragma unroll
-							for (int hy = 0; hy < PX; hy++) s += rowsq[ht][y + hy][x];
-						qn[y][x] = s;
+						for (int y = 0; y < kCH; y++)
+							if (y < ch) qn[y][x] = col[y];
 					}
 					__syncthreads();
 					// tensor-core cross terms: 8 candidates of one row per n-tile
@@ -288,8 +291,17 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 							const int ht0 = k0 / (PX * PX), hy0 = (k0 / PX) % PX, hx0 = k0 % PX;
 							const int k1 = k0 + 8;
 							const int ht1 = k1 / (PX * PX), hy1 = (k1 / PX) % PX, hx1 = k1 % PX;
-							const uint32_t b0 = *reinterpret_cast<const uint32_t *>(&win16[sh][ht0][y + hy0][xn - sh + hx0]);
-							const uint32_t b1 = *reinterpret_cast<const uint32_t *>(&win16[sh][ht1][y + hy1][xn - sh + hx1]);
+							uint32_t b0, b1;
+							if (!sh) {
+								b0 = *reinterpret_cast<const uint32_t *>(&win16[ht0][y + hy0][xn + hx0]);
+								b1 = *reinterpret_cast<const uint32_t *>(&win16[ht1][y + hy1][xn + hx1]);
+							} else {
+								// odd column: pack two 16-bit loads
+								const unsigned short *r0p = reinterpret_cast<const unsigned short *>(&win16[ht0][y + hy0][xn + hx0]);
+								const unsigned short *r1p = reinterpret_cast<const unsigned short *>(&win16[ht1][y + hy1][xn + hx1]);
+								b0 = (uint32_t)r0p[0] | ((uint32_t)r0p[1] << 16);
+								b1 = (uint32_t)r1p[0] | ((uint32_t)r1p[1] << 16);
+							}
 							mma16816(acc, afr[s], b0, b1);
 						}
 						// epilogue: rows r0, r0+8; columns 2*(lane&3), +1
@@ -399,8 +411,7 @@ size_t mixed_smem(const StepParams &sp)
 {
 	constexpr int WX = kCW + PX - 1, WY = kCH + PX - 1;
 	constexpr int WXP = (WX + 1 + 7) / 8 * 8;
-	return sizeof(__half) * 2 * PT * WY * WXP + sizeof(float) * (PT * WY * kCW + kCH * kCW) +
-	       sizeof(float) * kRefs * sp.wx * sp.wx;
+	return sizeof(__half) * PT * WY * WXP + sizeof(float) * kCH * kCW + sizeof(float) * kRefs * sp.wx * sp.wx;
 }
 
 template <int PX, int PT>
