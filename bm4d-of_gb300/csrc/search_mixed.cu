@@ -6,7 +6,7 @@
 // the reference's visiting order.  The squared distance is split as
 //     |p - q|^2 = |p'|^2 + |q'|^2 - 2 <p', q'>,   p' = p - 128, q' = q - 128,
 // with |q'|^2 in FP32 and <p', q'> on the tensor cores (FP16 operands, FP32
-// accumulation).  One CTA serves 16 reference patches of one grid row: each
+// accumulation).  One CTA serves a 4x4 block of reference patches: each
 // candidate frame's union of their windows is converted to FP16 once and fed
 // to mma.m16n8k16 as the B operand (16 references x 8 candidates x 16 patch
 // elements per instruction).  Every reference keeps its 2k best approximate
@@ -29,10 +29,11 @@ namespace bm4dof {
 namespace {
 
 constexpr int kRefs = 16;           // reference patches per CTA (the MMA M)
-constexpr int kThreads = 128;       // 4 warps
+constexpr int kBX = 4, kBY = 4;     // ... as a 4x4 block of grid positions
+constexpr int kThreads = 256;       // 8 warps
 constexpr int kTop = 32;            // approximate candidates kept per reference (2k)
-constexpr int kCW = 96;             // candidate columns per chunk (multiple of 8): 16 windows at offset 3
-constexpr int kCH = 24;             // candidate rows per chunk: one window plus flow spread
+constexpr int kCW = 40;             // candidate columns per chunk (multiple of 8): 4 windows at offset 3
+constexpr int kCH = 32;             // candidate rows per chunk
 constexpr float kShift = 128.f;     // values are centred before the FP16 conversion
 
 struct RefWin {
@@ -128,11 +129,13 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 	static_assert(K == 64, "mixed search expects 64-element patches");
 	constexpr int WX = kCW + PX - 1, WY = kCH + PX - 1;
 	constexpr int WXP = (WX + 1 + 7) / 8 * 8;                   // FP16 row pitch (16-byte rows)
+	constexpr int NW = kThreads / 32;
 	// dynamic shared memory: the chunk window in centred FP16 ([ht][y][x]),
-	// |q'|^2 of every chunk candidate, and the per-reference distances
+	// row sums of squares, |q'|^2 of every chunk candidate, per-reference distances
 	extern __shared__ __align__(16) unsigned char dsm[];
 	__half(*win16)[WY][WXP] = reinterpret_cast<__half(*)[WY][WXP]>(dsm);
-	float(*qn)[kCW] = reinterpret_cast<float(*)[kCW]>(dsm + sizeof(__half) * PT * WY * WXP);
+	float(*rowsq)[WY][kCW] = reinterpret_cast<float(*)[WY][kCW]>(dsm + sizeof(__half) * PT * WY * WXP);
+	float(*qn)[kCW] = reinterpret_cast<float(*)[kCW]>(reinterpret_cast<unsigned char *>(rowsq) + sizeof(float) * PT * WY * kCW);
 	float *distb = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(qn) + sizeof(float) * kCH * kCW);
 	const int wmax = sp.wx * sp.wx;
 #define dist(r, i) distb[(r) * wmax + (i)]
@@ -148,38 +151,40 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	for (long long bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
+		// a 4x4 block of reference positions of one frame
 		const long long g0 = a.blocks[bi];
 		const Tile T = a.tiles[tile_of(a.tiles, a.ntiles, g0)];
-		const int xi0 = (int)((g0 - T.g0) % T.nx);
-		const int nref = min(kRefs, T.nx - xi0);
+		const long long loc = g0 - T.g0;
+		const int xi0 = (int)(loc % T.nx), yi0 = (int)((loc / T.nx) % T.ny);
+		const int nbx = min(kBX, T.nx - xi0), nby = min(kBY, T.ny - yi0);
 		int xr, yr, tr;
 		group_xyz(T, a.grid, g0, xr, yr, tr);
 		int t0, t1;
 		trange(sp, tr, t0, t1);
 		const int nwt = t1 - t0 + 1;
 		if (tid < kRefs) {
-			const long long g = g0 + tid;
-			s_g[tid] = tid < nref ? g : -1;
-			if (tid < nref) {
-				int x, y, t;
-				group_xyz(T, a.grid, g, x, y, t);
-				s_x[tid] = x;
-				s_y[tid] = y;
-			}
+			const int dx = tid % kBX, dy = tid / kBX;
+			const bool ok = dx < nbx && dy < nby;
+			const long long g = g0 + (long long)dy * T.nx + dx;
+			s_g[tid] = ok ? g : -1;
+			int x = 0, y = 0, t;
+			if (ok) group_xyz(T, a.grid, g, x, y, t);
+			s_x[tid] = x;
+			s_y[tid] = y;
+			s_cbase[tid] = 0;
 		}
 		__syncthreads();
 		// reference patches: FP32 (re-rank) and centred FP16 (MMA A operand)
 		for (int i = tid; i < kRefs * K; i += blockDim.x) {
 			const int r = i / K, k = i % K;
 			float v = 0.f;
-			if (r < nref) {
+			if (s_g[r] >= 0) {
 				const int ht = k / (PX * PX), hy = (k / PX) % PX, hx = k % PX;
 				v = src.p[src.at(T.ox + s_x[r] + hx, T.oy + s_y[r] + hy, tr + ht, 0)];
 			}
 			ref32[r][k] = v;
 			ref16[r][k] = __float2half_rn(v - kShift);
 		}
-		// running lists: empty
 		for (int i = tid; i < kRefs * kTop; i += blockDim.x) {
 			s_ld[i / kTop][i % kTop] = __int_as_float(0x7f800000);
 			s_lc[i / kTop][i % kTop] = 0x7fffffff;
@@ -205,14 +210,13 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 			afr[s][2] = *reinterpret_cast<const uint32_t *>(&ref16[r0][c0 + 8]);
 			afr[s][3] = *reinterpret_cast<const uint32_t *>(&ref16[r0 + 8][c0 + 8]);
 		}
-		if (tid < kRefs) s_cbase[tid] = 0;
 
 		for (int ii = 0; ii < nwt; ii++) {
 			const int qt = visit(ii, tr, t1);
 			// own windows of this frame
 			if (tid < kRefs) {
 				RefWin w = {0, 0, 0, 0};
-				if (tid < nref) {
+				if (s_g[tid] >= 0) {
 					const uint32_t c = a.traj[(s_g[tid]) * a.nfm + ii];
 					const int cx = (int)(c & 0xffffu), cy = (int)(c >> 16);
 					const int hw = (sp.wx - 1) / 2;
@@ -226,9 +230,11 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 				rw[tid] = w;
 			}
 			__syncthreads();
-			// union box of the own windows
+			// this lane's two references (MMA rows lane/4 and lane/4 + 8)
+			const RefWin wa = rw[lane >> 2], wb = rw[(lane >> 2) + 8];
+			const float pna = pn[lane >> 2], pnb = pn[(lane >> 2) + 8];
 			int ux0 = 1 << 30, uy0 = 1 << 30, ux1 = -1, uy1 = -1;
-			for (int r = 0; r < nref; r++)
+			for (int r = 0; r < kRefs; r++)
 				if (rw[r].nx > 0 && rw[r].ny > 0) {
 					ux0 = min(ux0, rw[r].rx0);
 					uy0 = min(uy0, rw[r].ry0);
@@ -238,90 +244,83 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 			for (int cy0 = uy0; cy0 <= uy1; cy0 += kCH)
 				for (int cx0 = ux0; cx0 <= ux1; cx0 += kCW) {
 					const int cw = min(kCW, ux1 - cx0 + 1), ch = min(kCH, uy1 - cy0 + 1);
-					// chunk pixels -> centred FP16: one warp per row, lanes along x
 					const int ww = cw + PX - 1, hh = ch + PX - 1;
-					for (int row = warp; row < PT * hh; row += kThreads / 32) {
+					// chunk pixels -> centred FP16: one warp per row, lanes along x
+					for (int row = warp; row < PT * hh; row += NW) {
 						const int ht = row / hh, y = row - ht * hh;
 						const float *gp = src.p + src.at(T.ox + cx0, T.oy + cy0 + y, qt + ht, 0);
 						__half *dp = &win16[ht][y][0];
 						for (int x = lane; x < ww; x += 32) dp[x] = __float2half_rn(__ldg(gp + x) - kShift);
 					}
 					__syncthreads();
-					// |q'|^2 of every candidate from the rounded values: each thread
-					// slides a PX-row window down one candidate column
-					for (int x = tid; x < cw; x += kThreads) {
-						float col[kCH];
+					// row sums of squares of the rounded values
+					for (int row = warp; row < PT * hh; row += NW) {
+						const int ht = row / hh, y = row - ht * hh;
+						for (int x = lane; x < cw; x += 32) {
+							float sq = 0.f;
 #pragma unroll
-						for (int y = 0; y < kCH; y++) col[y] = 0.f;
-#pragma unroll
-						for (int ht = 0; ht < PT; ht++) {
-							float rs[kCH + PX - 1];
-#pragma unroll
-							for (int y = 0; y < kCH + PX - 1; y++) {
-								float sq = 0.f;
-								if (y < hh)
-#pragma unroll
-									for (int hx = 0; hx < PX; hx++) {
-										const float v = __half2float(win16[ht][y][x + hx]);
-										sq = fmaf(v, v, sq);
-									}
-								rs[y] = sq;
+							for (int hx = 0; hx < PX; hx++) {
+								const float v = __half2float(win16[ht][y][x + hx]);
+								sq = fmaf(v, v, sq);
 							}
-#pragma unroll
-							for (int y = 0; y < kCH; y++)
-#pragma unroll
-								for (int hy = 0; hy < PX; hy++) col[y] += rs[y + hy];
+							rowsq[ht][y][x] = sq;
 						}
-#pragma unroll
-						for (int y = 0; y < kCH; y++)
-							if (y < ch) qn[y][x] = col[y];
 					}
+					__syncthreads();
+					for (int y = warp; y < ch; y += NW)
+						for (int x = lane; x < cw; x += 32) {
+							float sq = 0.f;
+#pragma unroll
+							for (int ht = 0; ht < PT; ht++)
+#pragma unroll
+								for (int hy = 0; hy < PX; hy++) sq += rowsq[ht][y + hy][x];
+							qn[y][x] = sq;
+						}
 					__syncthreads();
 					// tensor-core cross terms: 8 candidates of one row per n-tile
 					const int ntx = (cw + 7) / 8;
-					for (int nt = warp; nt < ntx * ch; nt += kThreads / 32) {
-						const int y = nt / ntx, xb = (nt % ntx) * 8;
-						const int n = lane >> 2;                 // candidate of this lane's B fragment
-						const int xn = min(xb + n, cw - 1);
-						const int sh = xn & 1;
+					for (int nt = warp; nt < ntx * ch; nt += NW) {
+						const int y = nt / ntx, xb = (nt - y * ntx) * 8;
+						const int xn = min(xb + (lane >> 2), cw - 1);   // this lane's B column
+						const bool odd = xn & 1;
 						float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
 						for (int s = 0; s < 4; s++) {
-							const int k0 = s * 16 + (lane & 3) * 2;
+							const int k0 = s * 16 + (lane & 3) * 2, k1 = k0 + 8;
 							const int ht0 = k0 / (PX * PX), hy0 = (k0 / PX) % PX, hx0 = k0 % PX;
-							const int k1 = k0 + 8;
 							const int ht1 = k1 / (PX * PX), hy1 = (k1 / PX) % PX, hx1 = k1 % PX;
 							uint32_t b0, b1;
-							if (!sh) {
+							if (!odd) {
 								b0 = *reinterpret_cast<const uint32_t *>(&win16[ht0][y + hy0][xn + hx0]);
 								b1 = *reinterpret_cast<const uint32_t *>(&win16[ht1][y + hy1][xn + hx1]);
 							} else {
 								// odd column: pack two 16-bit loads
-								const unsigned short *r0p = reinterpret_cast<const unsigned short *>(&win16[ht0][y + hy0][xn + hx0]);
-								const unsigned short *r1p = reinterpret_cast<const unsigned short *>(&win16[ht1][y + hy1][xn + hx1]);
-								b0 = (uint32_t)r0p[0] | ((uint32_t)r0p[1] << 16);
-								b1 = (uint32_t)r1p[0] | ((uint32_t)r1p[1] << 16);
+								const unsigned short *p0 = reinterpret_cast<const unsigned short *>(&win16[ht0][y + hy0][xn + hx0]);
+								const unsigned short *p1 = reinterpret_cast<const unsigned short *>(&win16[ht1][y + hy1][xn + hx1]);
+								b0 = (uint32_t)p0[0] | ((uint32_t)p0[1] << 16);
+								b1 = (uint32_t)p1[0] | ((uint32_t)p1[1] << 16);
 							}
 							mma16816(acc, afr[s], b0, b1);
 						}
-						// epilogue: rows r0, r0+8; columns 2*(lane&3), +1
-						const int r0 = lane >> 2;
+						// epilogue: rows lane/4 (wa) and lane/4 + 8 (wb), columns 2*(lane&3), +1
+						const int qy = cy0 + y;
 #pragma unroll
 						for (int e = 0; e < 4; e++) {
-							const int r = r0 + (e >= 2 ? 8 : 0);
 							const int cxl = xb + (lane & 3) * 2 + (e & 1);
-							if (r >= nref || cxl >= cw) continue;
-							const int qx = cx0 + cxl, qy = cy0 + y;
-							const RefWin w = rw[r];
+							if (cxl >= cw) continue;
+							const int qx = cx0 + cxl;
+							const RefWin &w = e < 2 ? wa : wb;
 							const int lx = qx - w.rx0, ly = qy - w.ry0;
-							if (lx < 0 || lx >= w.nx || ly < 0 || ly >= w.ny) continue;
-							dist(r, ly * w.nx + lx) = pn[r] + qn[y][cxl] - 2.f * acc[e];
+							if ((unsigned)lx >= (unsigned)w.nx || (unsigned)ly >= (unsigned)w.ny) continue;
+							const int r = (lane >> 2) + (e < 2 ? 0 : 8);
+							dist(r, ly * w.nx + lx) = (e < 2 ? pna : pnb) + qn[y][cxl] - 2.f * acc[e];
 						}
 					}
 					__syncthreads();
 				}
 			// fold this frame into the running 2k lists (one warp per reference)
-			for (int r = warp; r < nref; r += kThreads / 32) {
+			for (int r = warp; r < kRefs; r += NW) {
+				if (s_g[r] < 0) continue;
 				const RefWin w = rw[r];
 				const int nw = w.nx * w.ny;
 				float ld = s_ld[r][lane];
@@ -342,13 +341,13 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 			__syncthreads();
 		}
 		// exact FP32 re-rank of the 2k candidates, then the k best and tau
-		for (int r = warp; r < nref; r += kThreads / 32) {
+		for (int r = warp; r < kRefs; r += NW) {
+			if (s_g[r] < 0) continue;
 			const int c = s_lc[r][lane];
 			float dex = __int_as_float(0x7f800000);
 			int qx = 0, qy = 0, qtt = 0;
 			if (c != 0x7fffffff) {
-				// candidate number -> frame and window position (rebuild the
-				// frame windows of reference r in visiting order)
+				// candidate number -> frame and window position
 				int rem = c, jj = 0, rx0 = 0, ry0 = 0, nx = 1;
 				for (jj = 0; jj < nwt; jj++) {
 					const uint32_t tc = a.traj[s_g[r] * a.nfm + jj];
@@ -366,13 +365,18 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 				qtt = visit(jj, tr, t1);
 				qx = rx0 + rem % nx;
 				qy = ry0 + rem / nx;
+				float v[K];
+#pragma unroll
+				for (int k = 0; k < K; k++) {
+					const int ht = k / (PX * PX), hy = (k / PX) % PX, hx = k % PX;
+					v[k] = __ldg(src.p + src.at(T.ox + qx + hx, T.oy + qy + hy, qtt + ht, 0));
+				}
 				float acc = 0.f;
-				for (int ht = 0, k = 0; ht < PT; ht++)
-					for (int hy = 0; hy < PX; hy++)
-						for (int hx = 0; hx < PX; hx++, k++) {
-							const float dd = __fsub_rn(ref32[r][k], __ldg(src.p + src.at(T.ox + qx + hx, T.oy + qy + hy, qtt + ht, 0)));
-							acc = __fadd_rn(acc, __fmul_rn(dd, dd));
-						}
+#pragma unroll
+				for (int k = 0; k < K; k++) {
+					const float dd = __fsub_rn(ref32[r][k], v[k]);
+					acc = __fadd_rn(acc, __fmul_rn(dd, dd));
+				}
 				dex = acc;
 			}
 			// sort by (exact distance, candidate number)
@@ -391,11 +395,13 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 			const int ncand = s_cbase[r];
 			const int Kk = min(sp.np, ncand);
 			// tau rule on the sorted exact distances
-			const float d1 = __shfl_sync(0xffffffffu, d, 1), d2 = __shfl_sync(0xffffffffu, d, 2);
-			const float d4 = __shfl_sync(0xffffffffu, d, 4), d8 = __shfl_sync(0xffffffffu, d, 8);
-			const float d16 = __shfl_sync(0xffffffffu, d, 16);
+			float dn[5];
+			dn[0] = __shfl_sync(0xffffffffu, d, 1);
+			dn[1] = __shfl_sync(0xffffffffu, d, 2);
+			dn[2] = __shfl_sync(0xffffffffu, d, 4);
+			dn[3] = __shfl_sync(0xffffffffu, d, 8);
+			dn[4] = __shfl_sync(0xffffffffu, d, 16);
 			int nS = 1;
-			const float dn[5] = {d1, d2, d4, d8, d16};
 			for (int q = 0; q < 5 && 2 * nS <= Kk && dn[q] < sp.tau2; q++) nS *= 2;
 			const long long g = s_g[r];
 			if (lane == 0) a.nsimp[g] = (uint8_t)nS;
@@ -411,7 +417,8 @@ size_t mixed_smem(const StepParams &sp)
 {
 	constexpr int WX = kCW + PX - 1, WY = kCH + PX - 1;
 	constexpr int WXP = (WX + 1 + 7) / 8 * 8;
-	return sizeof(__half) * PT * WY * WXP + sizeof(float) * kCH * kCW + sizeof(float) * kRefs * sp.wx * sp.wx;
+	return sizeof(__half) * PT * WY * WXP + sizeof(float) * (PT * WY * kCW + kCH * kCW) +
+	       sizeof(float) * kRefs * sp.wx * sp.wx;
 }
 
 template <int PX, int PT>
@@ -431,14 +438,14 @@ cudaError_t launch_mixed_t(const Image &src, const StepParams &sp, const MixedAr
 
 }  // namespace
 
-// First group of every run of up to 16 consecutive references of one grid row.
+// First group of every 4x4 block of reference positions of one frame.
 void mixed_blocks(const std::vector<Tile> &tiles, std::vector<long long> &out)
 {
 	out.clear();
 	for (const Tile &T : tiles)
 		for (int f = 0; f < T.nf; f++)
-			for (int y = 0; y < T.ny; y++)
-				for (int x = 0; x < T.nx; x += kRefs)
+			for (int y = 0; y < T.ny; y += kBY)
+				for (int x = 0; x < T.nx; x += kBX)
 					out.push_back(T.g0 + ((long long)f * T.ny + y) * T.nx + x);
 }
 
