@@ -94,9 +94,25 @@ __global__ void kill_apply_kernel(const unsigned long long *__restrict__ edges, 
 __global__ void count_alive_kernel(const Tile *__restrict__ tiles, int ntiles, long long G,
                                    const uint8_t *__restrict__ alive, unsigned *__restrict__ counts)
 {
+	// per-thread counts of the current tile, then one atomic per group of
+	// lanes holding the same tile (one counter per tile: plain per-group
+	// atomics serialise on it)
+	int ct = -1;
+	unsigned cnt = 0;
 	for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < G;
-	     g += (long long)gridDim.x * blockDim.x)
-		if (alive[g]) atomicAdd(&counts[tile_of(tiles, ntiles, g)], 1u);
+	     g += (long long)gridDim.x * blockDim.x) {
+		if (!alive[g]) continue;
+		const int t = tile_of(tiles, ntiles, g);
+		if (t != ct) {
+			if (cnt) atomicAdd(&counts[ct], cnt);
+			ct = t;
+			cnt = 0;
+		}
+		cnt++;
+	}
+	const unsigned same = __match_any_sync(0xffffffffu, ct);
+	const unsigned total = __reduce_add_sync(same, cnt);
+	if (ct >= 0 && total && (threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&counts[ct], total);
 }
 
 // ---------------------------------------------------------------------------
