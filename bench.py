@@ -162,12 +162,108 @@ def run_reference(args):
     return 0
 
 
+SIGMAS = (5.0, 10.0, 20.0, 30.0, 40.0, 50.0)
+
+
+def batch_specs(n, seed=4):
+    """Uneven batch: widths in [320, 1920], heights in [240, 1080] (multiples of
+    8), 5..30 frames, sigma from {5, 10, 20, 30, 40, 50}, each sequence with its
+    own seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        W = int(rng.integers(40, 241)) * 8
+        H = int(rng.integers(30, 136)) * 8
+        F = int(rng.integers(5, 31))
+        out.append((W, H, F, float(rng.choice(SIGMAS)), 1000 * seed + i))
+    return out
+
+
+def run_batch(args):
+    """Many sequences in one CUDA graph (bm4dof_run_batched), tuned by the
+    library's autotuner on a sample of the batch."""
+    import torch
+    import bm4dof
+    import synthetic
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    ctx = bm4dof.Context(local)
+    specs = batch_specs(args.batch_n)
+    items, host = [], []
+    for (W, H, F, sigma, seed) in specs:
+        clean, ff, bf = synthetic.video(W, H, F, seed)
+        nz = synthetic.noisy(clean, sigma, seed)
+        p1, p2 = resolve(bm4dof, W, H, F, sigma)
+        h = [torch.from_numpy(a).pin_memory() for a in (nz, ff, bf)]
+        d = [t.cuda() for t in h]
+        items.append({"noisy": d[0], "fflow": d[1], "bflow": d[2], "basic": torch.empty_like(d[0]),
+                      "final": torch.empty_like(d[0]), "p1": p1, "p2": p2, "nparts": args.nparts})
+        host.append(h + [torch.empty_like(h[0]).pin_memory()])
+    mpf = sum(W * H * F for (W, H, F, _, _) in specs) / 1e6
+    best, table = ctx.autotune(items, sample=min(8, len(items)))
+    for _ in range(max(args.warmup, 3)):
+        ctx.run_batched(items, tuning=best)
+    tms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            ctx.run_batched(items, tuning=best)
+            tms.append(ctx.timings()[0][4])
+    ms_step = statistics.mean(tms)
+    launches = ctx.timings()[1]
+    # per-sequence agreement with the unbatched plain path (the smallest four)
+    order = sorted(range(len(specs)), key=lambda i: specs[i][0] * specs[i][1] * specs[i][2])[:4]
+    agree = 0
+    for i in order:
+        it = items[i]
+        _, f, _ = ctx.runNlBayes(it["noisy"], it["fflow"], it["bflow"], it["p1"], it["p2"], nparts=args.nparts)
+        agree += bool(torch.equal(f, it["final"]))
+    # end to end: host inputs copied in and finals copied out inside the timed region
+    e2e = []
+    h2d = sum(sum(t.numel() * 4 for t in h[:3]) for h in host)
+    d2h = sum(h[3].numel() * 4 for h in host)
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for it, h in zip(items, host):
+            it["noisy"].copy_(h[0], non_blocking=True)
+            it["fflow"].copy_(h[1], non_blocking=True)
+            it["bflow"].copy_(h[2], non_blocking=True)
+        torch.cuda.synchronize()
+        ctx.run_batched(items, tuning=best)
+        for it, h in zip(items, host):
+            h[3].copy_(it["final"], non_blocking=True)
+        torch.cuda.synchronize()
+        e2e.append(time.perf_counter() - t0)
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": world * mpf / (ms_step / 1e3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (per-sequence seeded cosine+rectangle texture, motion, exact flow, AWGN)",
+        "config": {"workload": f"batch of {len(specs)} grey sequences, W in [320,1920], H in [240,1080], "
+                               f"5..30 frames, sigma in {{5..50}}, plain two-step FP32, one CUDA graph",
+                   "sequences": len(specs), "megapixel_frames": mpf, "tuning": best,
+                   "autotune": [list(r) for r in table], "parallelism": f"replicas x{world}"},
+        "roofline": None,
+        "e2e": {"value": world * mpf / statistics.mean(e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches, "clocks": clk.summary(),
+        "agreement_with_unbatched": f"{agree}/{len(order)} sequences bit-identical",
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def config(args):
     W, H, F, sigma, seed = WORKLOADS[args.workload]
+    mb = W * H * F * 4 * 5 / 1e6   # noisy + two 2-channel flows
     return {"workload": f"grey video {W}x{H}x{F}, sigma {sigma:g}, plain two-step FP32",
             "W": W, "H": H, "frames": F, "sigma": sigma, "seed": seed, "patch": "4x4x4",
             "n_similar": 16, "search": "21x21, +-4 frames along the flow", "tiles": args.nparts,
-            "l2": "inputs 2.5 GB > 129 MB L2 (no flush)", "parallelism": f"replicas x{args.gpus}"}
+            "l2": f"inputs {mb:.0f} MB > 129 MB L2 (no flush)" if mb > 129 else f"inputs {mb:.0f} MB",
+            "parallelism": f"replicas x{args.gpus}"}
 
 
 def main():
@@ -176,12 +272,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="hd", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="hd", choices=sorted(WORKLOADS) + ["batch"])
+    ap.add_argument("--batch-n", type=int, default=64, help="sequences of the batch workload")
     ap.add_argument("--nparts", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true", help="skip the host-core baseline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
 
     import torch
     import bm4dof
@@ -289,7 +388,13 @@ def main():
     # the faster forms of the same workload, timed the same way, with their
     # PSNR loss against the plain method
     forms = {}
-    for name, kw in (("mixed", {"mixed": True}),):
+    import train_gains
+    gains = train_gains.load_weights()
+    variants = [("mixed", {"mixed": True})]
+    if gains is not None:
+        ctx.set_gain_network(gains)
+        variants += [("learned", {"learned": True}), ("learned+mixed", {"learned": True, "mixed": True})]
+    for name, kw in variants:
         for _ in range(2):
             ctx.runNlBayes(d_nz, d_ff, d_bf, p1, p2, basic=d_basic, final=d_final, nparts=args.nparts, **kw)
         tms = []
@@ -299,9 +404,13 @@ def main():
             tms.append(ms[4])
         fq = psnr(d_final.cpu().numpy(), clean)
         forms[name] = {"value": world * mpf / (statistics.mean(tms) / 1e3), "unit": UNIT,
-                       "ms_per_step": statistics.mean(tms), "stage_ms": dict(zip(
-                           ("search", "filter", "aggregation", "other", "total"), ctx.timings()[0])),
+                       "ms_per_step": statistics.mean(tms), "speedup_vs_plain": ms_step / statistics.mean(tms),
+                       "stage_ms": dict(zip(("search", "filter", "aggregation", "other", "total"),
+                                            ctx.timings()[0])),
                        "psnr_db": fq, "psnr_loss_vs_plain_db": line["quality_db"]["final"] - fq}
+        if kw.get("learned"):
+            g, fb = ctx.learned_stats()
+            forms[name]["fallback_groups"] = [fb, g]
     line["forms"] = forms
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(nz, ff, bf, sigma)

@@ -23,6 +23,8 @@ LIB_PATH = os.path.join(HERE, "lib", "libbm4dof_gpu.so")
 DEVICE_POINTERS = 0x1
 KEEP_GROUPS = 0x2
 MIXED_PRECISION = 0x4
+LEARNED = 0x8
+GAIN_PARAMS = 99136   # floats in a gain-network parameter blob
 
 DCT, BIOR1_5 = 0, 1
 RGB, YUV = 0, 1
@@ -39,6 +41,10 @@ EXPORTS = [
     "bm4dof_set_n_similar_patches", "bm4dof_format_params", "bm4dof_print_params",
     "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run",
     "bm4dof_get_groups", "bm4dof_last_timings", "bm4dof_search_groups_noalloc",
+    "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_gain_samples",
+    "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_params", "bm4dof_trainer_grad",
+    "bm4dof_trainer_step", "bm4dof_trainer_predict", "bm4dof_run_batched", "bm4dof_autotune",
+    "bm4dof_tvl1_default_params", "bm4dof_tvl1_pairs", "bm4dof_tvl1_video",
 ]
 
 
@@ -72,6 +78,30 @@ class Params(C.Structure):
 
 class VideoSize(C.Structure):
     _fields_ = [("width", C.c_uint), ("height", C.c_uint), ("frames", C.c_uint), ("channels", C.c_uint)]
+
+
+class Sequence(C.Structure):
+    """bm4dof_sequence: one sequence of a batched run (device pointers)."""
+    _fields_ = [
+        ("noisy", C.c_void_p), ("fflow", C.c_void_p), ("bflow", C.c_void_p),
+        ("width", C.c_uint), ("height", C.c_uint), ("channels", C.c_uint), ("frames", C.c_uint),
+        ("basic", C.c_void_p), ("final_", C.c_void_p), ("params1", Params), ("params2", Params),
+        ("nparts", C.c_uint), ("ratios", C.c_float * 2),
+    ]
+
+
+class Tuning(C.Structure):
+    """bm4dof_tuning: launch shape of a batched run."""
+    _fields_ = [("branches", C.c_uint), ("slot_mb", C.c_uint), ("search_ctas", C.c_uint)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tvl1Params(C.Structure):
+    """bm4dof_tvl1_params (lib/tvl1flow's arguments)."""
+    _fields_ = [("tau", C.c_float), ("lambda_", C.c_float), ("theta", C.c_float), ("nscales", C.c_int),
+                ("fscale", C.c_int), ("zfactor", C.c_float), ("warps", C.c_int), ("epsilon", C.c_float)]
 
 
 _lib = None
@@ -116,6 +146,41 @@ def load(path: str = LIB_PATH):
         C.POINTER(Params), C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint, C.c_size_t,
         C.POINTER(C.c_size_t), C.c_void_p]
     L.bm4dof_search_groups_noalloc.restype = C.c_int
+    L.bm4dof_run_batched.argtypes = [C.c_void_p, C.POINTER(Sequence), C.c_uint, C.c_uint, C.POINTER(Tuning)]
+    L.bm4dof_run_batched.restype = C.c_int
+    L.bm4dof_autotune.argtypes = [C.c_void_p, C.POINTER(Sequence), C.c_uint, C.c_uint, C.c_uint,
+                                  C.POINTER(Tuning), C.POINTER(C.c_float), C.c_uint, C.POINTER(C.c_uint)]
+    L.bm4dof_autotune.restype = C.c_int
+    L.bm4dof_tvl1_default_params.argtypes = [C.POINTER(Tvl1Params)]
+    L.bm4dof_tvl1_default_params.restype = None
+    L.bm4dof_tvl1_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint, C.c_uint, C.c_uint,
+                                    C.POINTER(Tvl1Params), C.c_void_p, C.c_uint]
+    L.bm4dof_tvl1_pairs.restype = C.c_int
+    L.bm4dof_tvl1_video.argtypes = [C.c_void_p, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.POINTER(Tvl1Params),
+                                    C.c_void_p, C.c_void_p, C.c_uint]
+    L.bm4dof_tvl1_video.restype = C.c_int
+    L.bm4dof_set_gain_network.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float]
+    L.bm4dof_set_gain_network.restype = C.c_int
+    L.bm4dof_learned_stats.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]
+    L.bm4dof_learned_stats.restype = C.c_int
+    L.bm4dof_gain_samples.argtypes = [C.c_void_p] * 5 + [C.c_uint] * 3 + [
+        C.POINTER(Params), C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+        C.POINTER(C.c_size_t)]
+    L.bm4dof_gain_samples.restype = C.c_int
+    L.bm4dof_trainer_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_uint, C.c_uint]
+    L.bm4dof_trainer_create.restype = C.c_int
+    L.bm4dof_trainer_destroy.argtypes = [C.c_void_p]
+    L.bm4dof_trainer_destroy.restype = None
+    L.bm4dof_trainer_params.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    L.bm4dof_trainer_params.restype = C.c_int
+    L.bm4dof_trainer_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint, C.c_void_p,
+                                      C.POINTER(C.c_float)]
+    L.bm4dof_trainer_grad.restype = C.c_int
+    L.bm4dof_trainer_step.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint, C.c_float, C.c_float,
+                                      C.POINTER(C.c_float)]
+    L.bm4dof_trainer_step.restype = C.c_int
+    L.bm4dof_trainer_predict.argtypes = [C.c_void_p, C.c_void_p, C.c_uint, C.c_void_p]
+    L.bm4dof_trainer_predict.restype = C.c_int
     _lib = L
     return L
 
@@ -160,6 +225,34 @@ def version() -> str:
     return load().bm4dof_version().decode()
 
 
+def cli_params(size, sigma, px1=-1, px2=-1, pt1=1, pt2=1, wx1=-1, wx2=-1, np1=-1, np2=-1, b1=-1.0,
+               b2=-1.0, bm1=-1.0, bm2=-1.0, no_step1=False, no_step2=False, order_inv=False, verbose=False):
+    """Parameters of both steps as the reference CLI resolves them from its
+    flags (src/main_vnlb.cpp:206-246; -t1/-t2 only apply under VBM3D_SEARCH,
+    -wt1/-wt2 never).  size = (width, height, frames, channels); -1 = flag
+    not given."""
+    p1 = initializeNlbParameters(1, sigma, size, verbose)
+    p2 = initializeNlbParameters(2, sigma, size, verbose)
+    if wx1 >= 0: setSizeSearchWindow(p1, wx1)
+    if wx2 >= 0: setSizeSearchWindow(p2, wx2)
+    if px1 >= 0: setSizePatch(p1, size, px1)
+    if px2 >= 0: setSizePatch(p2, size, px2)
+    if np1 >= 0: setNSimilarPatches(p1, np1)
+    if np2 >= 0: setNSimilarPatches(p2, np2)
+    if b1 >= 0: p1.beta = b1; p1.betaMean = b1
+    if b2 >= 0: p2.beta = b2; p2.betaMean = b2
+    if bm1 >= 0: p1.betaMean = bm1
+    if bm2 >= 0: p2.betaMean = bm2
+    if pt1 >= 0: p1.sizePatchTime = pt1
+    if pt2 >= 0: p2.sizePatchTime = pt2
+    if no_step1: p1.offSet = 1
+    if no_step2: p2.offSet = 1
+    if order_inv:
+        p1.orderInvariance = 1
+        p2.orderInvariance = 1
+    return p1, p2
+
+
 # ---- device context ----------------------------------------------------------
 
 def _is_cuda_tensor(x):
@@ -186,12 +279,15 @@ class Context:
             pass
 
     def runNlBayes(self, noisy, fflow, bflow, p1, p2, basic=None, nparts=2, keep_groups=False,
-                   final=None, mixed=False):
+                   final=None, mixed=False, learned=False):
         """VideoNLB::runNlBayes.  Returns (basic, final, (ratio1, ratio2)).
 
         With CUDA tensors the inputs stay on the device and basic/final are
-        CUDA tensors (pass preallocated ones to avoid allocation)."""
+        CUDA tensors (pass preallocated ones to avoid allocation).
+        learned=True runs the learned form (no step-1 pass; the gain network
+        installed by set_gain_network, or none)."""
         flags = (KEEP_GROUPS if keep_groups else 0) | (MIXED_PRECISION if mixed else 0)
+        flags |= LEARNED if learned else 0
         if _is_cuda_tensor(noisy):
             import torch
             F, Cc, H, W = noisy.shape
@@ -232,6 +328,123 @@ class Context:
         _check(L.bm4dof_get_groups(self._h, step, tile, up(ref), up(ns), up(idx), stride, cnt, C.byref(n)))
         return {"ref": ref, "nsimp": ns, "index": idx.reshape(cnt, stride)}
 
+    @staticmethod
+    def _sequences(items):
+        """items: dicts with CUDA tensors noisy, fflow, bflow (or None), basic,
+        final (F, C, H, W) and params p1, p2 (and optional nparts)."""
+        arr = (Sequence * len(items))()
+        for q, it in zip(arr, items):
+            F, Cc, H, W = it["noisy"].shape
+            ptr = lambda t: t.data_ptr() if t is not None else None
+            q.noisy, q.fflow, q.bflow = ptr(it["noisy"]), ptr(it.get("fflow")), ptr(it.get("bflow"))
+            q.width, q.height, q.channels, q.frames = W, H, Cc, F
+            q.basic, q.final_ = ptr(it["basic"]), ptr(it["final"])
+            q.params1, q.params2 = it["p1"], it["p2"]
+            q.nparts = it.get("nparts", 2)
+        return arr
+
+    def run_batched(self, items, mixed=False, learned=False, tuning=None):
+        """Denoise many sequences with one CUDA graph (bm4dof_run_batched).
+        Returns the per-sequence ratios."""
+        arr = self._sequences(items)
+        flags = (MIXED_PRECISION if mixed else 0) | (LEARNED if learned else 0)
+        t = None
+        if tuning is not None:
+            t = Tuning(**tuning) if isinstance(tuning, dict) else tuning
+        _check(load().bm4dof_run_batched(self._h, arr, len(items), flags, C.byref(t) if t is not None else None))
+        return [(q.ratios[0], q.ratios[1]) for q in arr]
+
+    def autotune(self, items, sample=16, mixed=False, learned=False):
+        """(best tuning dict, table of (branches, slot_mb, search_ctas, ms))."""
+        arr = self._sequences(items)
+        flags = (MIXED_PRECISION if mixed else 0) | (LEARNED if learned else 0)
+        best = Tuning()
+        table = (C.c_float * (4 * 32))()
+        rows = C.c_uint()
+        _check(load().bm4dof_autotune(self._h, arr, len(items), sample, flags, C.byref(best), table, 32,
+                                      C.byref(rows)))
+        tab = [tuple(table[4 * i:4 * i + 4]) for i in range(min(rows.value, 32))]
+        return best.as_dict(), tab
+
+    def set_gain_network(self, params=None, kappa=0.0):
+        """Install the gain network (float blob of GAIN_PARAMS values) for
+        learned runs; None runs the learned form without it."""
+        if params is None:
+            _check(load().bm4dof_set_gain_network(self._h, None, 0, kappa))
+            return
+        a = np.ascontiguousarray(params, np.float32).ravel()
+        _check(load().bm4dof_set_gain_network(self._h, C.c_void_p(a.ctypes.data), a.size, kappa))
+
+    def learned_stats(self):
+        """(groups, fallback groups) of the last learned run."""
+        g, f = C.c_ulonglong(), C.c_ulonglong()
+        _check(load().bm4dof_learned_stats(self._h, C.byref(g), C.byref(f)))
+        return g.value, f.value
+
+    def gain_samples(self, noisy, basic, fflow, bflow, p2, nparts=2):
+        """Training pairs of the gain network for one grey video (CUDA
+        tensors (F, 1, H, W)): returns (features [n, 65], targets [n, 64]) as
+        CUDA tensors, the groups the filter processes only."""
+        import torch
+        F, Cc, H, W = noisy.shape
+        dev = noisy.device
+        L = load()
+        n = C.c_size_t()
+        cap = 1
+        while True:
+            feat = torch.empty((cap, 65), dtype=torch.float32, device=dev)
+            tgt = torch.empty((cap, 64), dtype=torch.float32, device=dev)
+            valid = torch.empty((cap,), dtype=torch.uint8, device=dev)
+            ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+            code = L.bm4dof_gain_samples(self._h, ptr(noisy.contiguous()), ptr(basic.contiguous()),
+                                         ptr(fflow), ptr(bflow), W, H, F, C.byref(p2), nparts,
+                                         DEVICE_POINTERS, ptr(feat), ptr(tgt), ptr(valid), cap, C.byref(n))
+            if code == 1 and n.value > cap:
+                cap = n.value
+                continue
+            _check(code)
+            break
+        keep = valid[: n.value].bool()
+        return feat[: n.value][keep], tgt[: n.value][keep]
+
+    @staticmethod
+    def tvl1_params(**kw):
+        """bm4dof_tvl1_params with the tvl1flow-seq.sh defaults, overridden by kw."""
+        p = Tvl1Params()
+        load().bm4dof_tvl1_default_params(C.byref(p))
+        for k, v in kw.items():
+            setattr(p, "lambda_" if k == "lambda" else k, v)
+        return p
+
+    def tvl1_pairs(self, I0, I1, params=None):
+        """TV-L1 flow of frame pairs (numpy [n, H, W] or [H, W] float32):
+        returns [n, 2, H, W] (u, v)."""
+        a = np.ascontiguousarray(I0, np.float32)
+        b = np.ascontiguousarray(I1, np.float32)
+        single = a.ndim == 2
+        if single:
+            a, b = a[None], b[None]
+        n, H, W = a.shape
+        uv = np.zeros((n, 2, H, W), np.float32)
+        p = params or self.tvl1_params()
+        _check(load().bm4dof_tvl1_pairs(self._h, C.c_void_p(a.ctypes.data), C.c_void_p(b.ctypes.data), W, H, n,
+                                        C.byref(p), C.c_void_p(uv.ctypes.data), 0))
+        return uv[0] if single else uv
+
+    def tvl1_video(self, video, params=None):
+        """Forward and backward flows (F, 2, H, W) of a grey video (F, 1, H, W)
+        or (F, H, W), in the layout runNlBayes takes."""
+        v = np.ascontiguousarray(video, np.float32)
+        if v.ndim == 4:
+            v = np.ascontiguousarray(v[:, 0])
+        F, H, W = v.shape
+        ff = np.zeros((F, 2, H, W), np.float32)
+        bf = np.zeros((F, 2, H, W), np.float32)
+        p = params or self.tvl1_params()
+        _check(load().bm4dof_tvl1_video(self._h, C.c_void_p(v.ctypes.data), W, H, F, C.byref(p),
+                                        C.c_void_p(ff.ctypes.data), C.c_void_p(bf.ctypes.data), 0))
+        return ff, bf
+
     def timings(self):
         """(ms_search, ms_filter, ms_aggregation, ms_other, ms_total), kernel launches."""
         ms = (C.c_float * 5)()
@@ -249,3 +462,69 @@ def runNlBayes(noisy, fflow, bflow, p1, p2, basic=None, nparts=2, **kw):
     if _default is None:
         _default = Context(0)
     return _default.runNlBayes(noisy, fflow, bflow, p1, p2, basic=basic, nparts=nparts, **kw)
+
+
+class Trainer:
+    """GPU training of the gain network (bm4dof_trainer_*): BF16 forward and
+    backward with FP32 accumulation, AdamW on FP32 master weights.  Features
+    and targets are CUDA float tensors [n, 65] and [n, 64], n <= batch."""
+
+    def __init__(self, batch=8192, device=0, seed=0):
+        self._h = C.c_void_p()
+        _check(load().bm4dof_trainer_create(C.byref(self._h), device, batch, seed))
+        self.batch = batch
+
+    def close(self):
+        if self._h:
+            load().bm4dof_trainer_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        a = np.zeros(GAIN_PARAMS, np.float32)
+        _check(load().bm4dof_trainer_params(self._h, C.c_void_p(a.ctypes.data), a.size, 0))
+        return a
+
+    def set_params(self, a):
+        a = np.ascontiguousarray(a, np.float32).ravel()
+        _check(load().bm4dof_trainer_params(self._h, C.c_void_p(a.ctypes.data), a.size, 1))
+
+    def grad(self, feat, target):
+        g = np.zeros(GAIN_PARAMS, np.float32)
+        loss = C.c_float()
+        _check(load().bm4dof_trainer_grad(self._h, C.c_void_p(feat.data_ptr()), C.c_void_p(target.data_ptr()),
+                                          feat.shape[0], C.c_void_p(g.ctypes.data), C.byref(loss)))
+        return g, loss.value
+
+    def step(self, feat, target, lr=1e-3, weight_decay=1e-4, want_loss=True):
+        """One AdamW step; returns the batch loss (before the update) when
+        want_loss, else None (no host synchronisation)."""
+        loss = C.c_float()
+        _check(load().bm4dof_trainer_step(self._h, C.c_void_p(feat.data_ptr()), C.c_void_p(target.data_ptr()),
+                                          feat.shape[0], lr, weight_decay, C.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def predict(self, feat):
+        import torch
+        out = torch.empty((feat.shape[0], 64), dtype=torch.float32, device=feat.device)
+        _check(load().bm4dof_trainer_predict(self._h, C.c_void_p(feat.data_ptr()), feat.shape[0],
+                                             C.c_void_p(out.data_ptr())))
+        return out
+
+
+def split_params(a):
+    """Views of a parameter blob: (W1[65,256], b1, W2[256,256], b2, W3[256,64], b3)."""
+    a = np.asarray(a, np.float32).ravel()
+    shapes = [(65, 256), (256,), (256, 256), (256,), (256, 64), (64,)]
+    out, o = [], 0
+    for sh in shapes:
+        n = int(np.prod(sh))
+        out.append(a[o:o + n].reshape(sh))
+        o += n
+    assert o == GAIN_PARAMS
+    return out

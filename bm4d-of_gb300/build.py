@@ -19,11 +19,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libbm4dof_gpu.so")
+CLI = os.path.join(OUT, "bm4dof")          # the command line, linked to LIB
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 SOURCES = ["search.cu", "search_mixed.cu", "filter.cu", "aggregate.cu", "runtime.cu", "noalloc.cu",
+           "mlp.cu", "learned.cu", "tvl1.cu",
            "params.cpp", "basis.cpp"]
 
 
@@ -61,6 +63,15 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    cli_src = os.path.join(SRC, "cli.cpp")
+    hdr = os.path.join(HERE, "..", "include", "bm4dof.h")
+    if not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(x) for x in (cli_src, hdr, LIB)):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", cli_src, "-o", CLI, "-L" + OUT, "-lbm4dof_gpu",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"cli build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

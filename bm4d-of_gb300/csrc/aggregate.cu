@@ -65,6 +65,39 @@ __global__ void kill_edges_kernel(const Tile *__restrict__ tiles, int ntiles,
 	}
 }
 
+// The switch-offs as a fixed point on the device: a victim is dead when a
+// live killer points at it; repeat until nothing changes (at most n + 1
+// rounds: every round that changes something settles at least one more
+// group).  One CTA, so that the rounds need only CTA barriers.
+__global__ void __launch_bounds__(1024)
+kill_fixpoint_kernel(const unsigned long long *__restrict__ edges, const unsigned *__restrict__ nedges,
+                     unsigned cap, uint8_t *__restrict__ alive, uint8_t *__restrict__ killed)
+{
+	__shared__ int changed;
+	const unsigned n = min(*nedges, cap);
+	for (unsigned round = 0; round <= n; round++) {
+		for (unsigned e = threadIdx.x; e < n; e += blockDim.x) killed[edges[e] & 0xffffffffull] = 0;
+		if (threadIdx.x == 0) changed = 0;
+		__syncthreads();
+		for (unsigned e = threadIdx.x; e < n; e += blockDim.x) {
+			const unsigned long long v = edges[e];
+			if (alive[v >> 32]) killed[v & 0xffffffffull] = 1;
+		}
+		__syncthreads();
+		for (unsigned e = threadIdx.x; e < n; e += blockDim.x) {
+			const long long w = (long long)(edges[e] & 0xffffffffull);
+			const uint8_t a = killed[w] ? 0 : 1;
+			if (alive[w] != a) {
+				alive[w] = a;
+				changed = 1;
+			}
+		}
+		__syncthreads();
+		if (!changed) break;
+		__syncthreads();
+	}
+}
+
 __global__ void kill_mark_kernel(const unsigned long long *__restrict__ edges, unsigned n,
                                  const uint8_t *__restrict__ alive, uint8_t *__restrict__ killed,
                                  int clear)
@@ -291,39 +324,46 @@ __global__ void slist_build_kernel(int w, int h, int F, int px_rt, int pt, int t
 // Ordered gather: each pixel merges the spatial lists of the pt origin frames
 // that cover it and adds the terms in slot order -- the order in which the
 // reference's scatter loop adds them.  PT > 0 keeps the pt list heads in
-// registers.
-template <int PT>
-__global__ void gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi,
-                                    const unsigned *__restrict__ soff, const unsigned *__restrict__ sl,
-                                    const float *__restrict__ vals, const float *__restrict__ wslot,
-                                    const float *__restrict__ win, float *__restrict__ acc,
-                                    float *__restrict__ wacc)
+// registers; CC is the channel count.  Each list's next entry is fetched one
+// step ahead, so that the load of the term being added and the list advance
+// overlap instead of forming one dependent chain per term.
+template <int PT, int CC>
+__global__ void __launch_bounds__(128)
+gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *__restrict__ soff,
+                    const unsigned *__restrict__ sl, const float *__restrict__ vals,
+                    const float *__restrict__ wslot, const float *__restrict__ win, float *__restrict__ acc,
+                    float *__restrict__ wacc)
 {
 	constexpr int L = PT > 0 ? PT : kMaxSpc;
-	const int px = sp.px, pt = PT > 0 ? PT : sp.pt, spc = sp.spc, C = sp.C;
+	const int px = sp.px, pt = PT > 0 ? PT : sp.pt, spc = sp.spc;
 	const size_t wh = (size_t)T.w * T.h;
 	const size_t n = wh * (size_t)(f_hi - f_lo + 1);
 	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
 		const int t = f_lo + (int)(i / wh);
 		const size_t xy = i % wh;
-		unsigned cur[L], end[L], head[L];
+		unsigned cur[L], end[L], head[L], nxt[L];
 		bool any = false;
 #pragma unroll
 		for (int dt = 0; dt < L; dt++) {
-			head[dt] = 0xffffffffu;
+			head[dt] = nxt[dt] = 0xffffffffu;
 			cur[dt] = end[dt] = 0;
 			const int to = t - dt;
 			if (dt < pt && to >= 0 && to <= sp.F - pt) {
 				const size_t q = (size_t)to * wh + xy;
 				cur[dt] = soff[q];
 				end[dt] = soff[q + 1];
-				if (cur[dt] < end[dt]) { head[dt] = sl[cur[dt]]; any = true; }
+				if (cur[dt] < end[dt]) {
+					head[dt] = sl[cur[dt]];
+					any = true;
+					if (cur[dt] + 1 < end[dt]) nxt[dt] = sl[cur[dt] + 1];
+				}
 			}
 		}
 		if (!any) continue;
 		const size_t pix = (size_t)t * wh + xy;
-		float a[4] = {0.f, 0.f, 0.f, 0.f};
-		for (int c = 0; c < C; c++) a[c] = acc[((size_t)t * C + c) * wh + xy];
+		float a[CC];
+#pragma unroll
+		for (int c = 0; c < CC; c++) a[c] = acc[((size_t)t * CC + c) * wh + xy];
 		float wa = wacc[pix];
 		for (;;) {
 			unsigned best = 0xffffffffu;
@@ -332,18 +372,41 @@ __global__ void gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi,
 			for (int l = 0; l < L; l++)
 				if (head[l] < best) { best = head[l]; bl = l; }
 			if (bl < 0) break;
-#pragma unroll
-			for (int l = 0; l < L; l++)
-				if (l == bl) head[l] = ++cur[l] < end[l] ? sl[cur[l]] : 0xffffffffu;
 			const unsigned slot = best >> 6;
 			const int dx = best & 7, dy = (best >> 3) & 7;
 			const int p = (bl * px + dy) * px + dx;
-			const float *v = vals + (size_t)slot * (C * spc) + p;
-			for (int c = 0; c < C; c++) a[c] = __fadd_rn(a[c], v[c * spc]);
-			wa = __fadd_rn(wa, __fmul_rn(wslot[slot], win[p]));
+			const float *v = vals + (size_t)slot * (CC * spc) + p;
+			float x[CC];
+#pragma unroll
+			for (int c = 0; c < CC; c++) x[c] = __ldg(v + c * spc);
+			const float ws = __ldg(wslot + slot);
+#pragma unroll
+			for (int l = 0; l < L; l++)
+				if (l == bl) {
+					head[l] = nxt[l];
+					cur[l]++;
+					nxt[l] = cur[l] + 1 < end[l] ? __ldg(sl + cur[l] + 1) : 0xffffffffu;
+				}
+#pragma unroll
+			for (int c = 0; c < CC; c++) a[c] = __fadd_rn(a[c], x[c]);
+			wa = __fadd_rn(wa, __fmul_rn(ws, win[p]));
 		}
 		wacc[pix] = wa;
-		for (int c = 0; c < C; c++) acc[((size_t)t * C + c) * wh + xy] = a[c];
+#pragma unroll
+		for (int c = 0; c < CC; c++) acc[((size_t)t * CC + c) * wh + xy] = a[c];
+	}
+}
+
+template <int CC>
+void gather_pt(int gb, cudaStream_t st, const Tile &T, const StepParams &sp, int t_lo, int f_hi,
+               const unsigned *soff, const unsigned *sl, const float *vals, const float *wslot, const float *win,
+               float *acc, float *wacc)
+{
+	switch (sp.pt) {
+	case 1: gather_slist_kernel<1, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
+	case 2: gather_slist_kernel<2, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
+	case 4: gather_slist_kernel<4, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
+	default: gather_slist_kernel<0, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
 	}
 }
 
@@ -459,6 +522,13 @@ cudaError_t launch_kill_iteration(const unsigned long long *edges, unsigned n, u
 	return cudaGetLastError();
 }
 
+cudaError_t launch_kill_fixpoint(const unsigned long long *edges, const unsigned *nedges, unsigned cap,
+                                 uint8_t *alive, uint8_t *killed, cudaStream_t st)
+{
+	kill_fixpoint_kernel<<<1, 1024, 0, st>>>(edges, nedges, cap, alive, killed);
+	return cudaGetLastError();
+}
+
 cudaError_t launch_count_alive(const Tile *tiles, int ntiles, long long G, const uint8_t *alive,
                                unsigned *counts, cudaStream_t st)
 {
@@ -517,12 +587,9 @@ cudaError_t launch_gather(const Tile &T, const StepParams &sp, int t_lo, int t_h
 	const int f_hi = t_hi + sp.pt - 1 < sp.F - 1 ? t_hi + sp.pt - 1 : sp.F - 1;
 	const long long npix = (long long)T.w * T.h * (f_hi - t_lo + 1);
 	const int gb = grid_for(npix, 128, 65535);
-	switch (sp.pt) {
-	case 1: gather_slist_kernel<1><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
-	case 2: gather_slist_kernel<2><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
-	case 4: gather_slist_kernel<4><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
-	default: gather_slist_kernel<0><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
-	}
+	if (sp.C == 1) gather_pt<1>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc);
+	else if (sp.C == 3) gather_pt<3>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc);
+	else gather_pt<4>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc);
 	return cudaGetLastError();
 }
 

@@ -1,0 +1,498 @@
+// cli.cpp -- the bm4d-of command line over the GPU library.
+//
+// Mirrors the reference's CLI (src/main_vnlb.cpp:31-253): the same flags,
+// defaults, checks, messages and parameter overrides, then one bm4dof_run.
+// Frame files are addressed by printf patterns with -f/-l/-s exactly as
+// Video<float>::loadVideo / saveVideo do (src/utils/lib_videot.cpp:30-126).
+//
+// File formats (the reference reads and writes through iio; this build reads
+// and writes the float formats itself and has no image libraries):
+//   .pfm  Portable Float Map: "Pf" grey or "PF" three channels, rows stored
+//         bottom to top, little endian when the scale is negative;
+//   .flo  Middlebury optical flow: "PIEH", int32 width and height, then
+//         interleaved (u, v) float32 pixels, top row first (the layout iio
+//         reads, lib/iio/iio.c:1885-1903);
+//   .png  output only: 8-bit grey or RGB, values rounded and clamped to
+//         [0, 255], stored (uncompressed) deflate blocks.
+// As the reference's loadImage does (src/utils/lib_image.cpp:66-73), a
+// three-channel frame whose channels are all equal is read as grey.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bm4dof.h"
+
+namespace {
+
+// ---- options (the reference's clo_option: "-name value", last one wins) ----
+struct Args {
+	int argc;
+	char **argv;
+	bool help = false;
+	const char *find(const char *name) const
+	{
+		const char *v = nullptr;
+		for (int i = 1; i + 1 < argc; i++)
+			if (!std::strcmp(argv[i], name)) v = argv[i + 1];
+		return v;
+	}
+	std::string str(const char *n, const char *d, const char *use)
+	{
+		usage(n, d, use);
+		const char *v = find(n);
+		return v ? v : d;
+	}
+	int i(const char *n, int d, const char *use)
+	{
+		usage(n, std::to_string(d).c_str(), use);
+		const char *v = find(n);
+		return v ? std::atoi(v) : d;
+	}
+	float f(const char *n, float d, const char *use)
+	{
+		char b[32];
+		std::snprintf(b, sizeof b, "%g", d);
+		usage(n, b, use);
+		const char *v = find(n);
+		if (!v) return d;
+		float x = 0.f, y = 1.f;   // "a/b" fractions, as the reference's atof
+		std::sscanf(v, "%g/%g", &x, &y);
+		return x / y;
+	}
+	void usage(const char *n, const char *d, const char *use)
+	{
+		if (help) std::printf("    %-12s = %-16s : %s\n", n, d, use);
+	}
+};
+
+// ---- frame files -------------------------------------------------------------
+bool ends_with(const std::string &s, const char *e)
+{
+	const size_t n = std::strlen(e);
+	return s.size() >= n && !s.compare(s.size() - n, n, e);
+}
+
+bool host_little_endian()
+{
+	const uint16_t v = 1;
+	unsigned char b[2];
+	std::memcpy(b, &v, 2);
+	return b[0] == 1;
+}
+
+void swap4(unsigned char *p)
+{
+	std::swap(p[0], p[3]);
+	std::swap(p[1], p[2]);
+}
+
+// planar (c, y, x) floats
+bool read_pfm(const char *path, std::vector<float> &out, int &w, int &h, int &c)
+{
+	FILE *f = std::fopen(path, "rb");
+	if (!f) return false;
+	char tag[3] = {0, 0, 0};
+	float scale = 0.f;
+	bool ok = std::fscanf(f, "%2s %d %d %f", tag, &w, &h, &scale) == 4 && w > 0 && h > 0;
+	if (ok) ok = std::fgetc(f) != EOF;   // the single whitespace before the data
+	c = tag[1] == 'F' ? 3 : 1;
+	ok = ok && tag[0] == 'P' && (tag[1] == 'F' || tag[1] == 'f');
+	std::vector<unsigned char> raw;
+	if (ok) {
+		raw.resize((size_t)w * h * c * 4);
+		ok = std::fread(raw.data(), 1, raw.size(), f) == raw.size();
+	}
+	std::fclose(f);
+	if (!ok) return false;
+	const bool swap = (scale < 0.f) != host_little_endian();
+	out.assign((size_t)w * h * c, 0.f);
+	for (int y = 0; y < h; y++)
+		for (int x = 0; x < w; x++)
+			for (int k = 0; k < c; k++) {
+				unsigned char *p = &raw[(((size_t)(h - 1 - y) * w + x) * c + k) * 4];   // bottom row first
+				if (swap) swap4(p);
+				std::memcpy(&out[((size_t)k * h + y) * w + x], p, 4);
+			}
+	return true;
+}
+
+bool write_pfm(const char *path, const float *planar, int w, int h, int c)
+{
+	FILE *f = std::fopen(path, "wb");
+	if (!f) return false;
+	std::fprintf(f, "%s\n%d %d\n%s\n", c == 3 ? "PF" : "Pf", w, h, host_little_endian() ? "-1.0" : "1.0");
+	std::vector<float> row((size_t)w * c);
+	bool ok = true;
+	for (int y = h - 1; y >= 0 && ok; y--) {
+		for (int x = 0; x < w; x++)
+			for (int k = 0; k < c; k++) row[(size_t)x * c + k] = planar[((size_t)k * h + y) * w + x];
+		ok = std::fwrite(row.data(), sizeof(float), row.size(), f) == row.size();
+	}
+	return std::fclose(f) == 0 && ok;
+}
+
+bool read_flo(const char *path, std::vector<float> &out, int &w, int &h, int &c)
+{
+	FILE *f = std::fopen(path, "rb");
+	if (!f) return false;
+	float magic = 0.f;
+	int32_t wh[2] = {0, 0};
+	bool ok = std::fread(&magic, 4, 1, f) == 1 && std::fread(wh, 4, 2, f) == 2 && magic == 202021.25f &&
+	          wh[0] > 0 && wh[1] > 0;
+	w = wh[0];
+	h = wh[1];
+	c = 2;
+	std::vector<float> raw;
+	if (ok) {
+		raw.resize((size_t)w * h * 2);
+		ok = std::fread(raw.data(), sizeof(float), raw.size(), f) == raw.size();
+	}
+	std::fclose(f);
+	if (!ok) return false;
+	out.assign(raw.size(), 0.f);
+	for (size_t p = 0; p < (size_t)w * h; p++) {
+		out[p] = raw[2 * p];
+		out[(size_t)w * h + p] = raw[2 * p + 1];
+	}
+	return true;
+}
+
+bool write_flo(const char *path, const float *planar, int w, int h)
+{
+	FILE *f = std::fopen(path, "wb");
+	if (!f) return false;
+	const float magic = 202021.25f;
+	const int32_t wh[2] = {w, h};
+	std::vector<float> raw((size_t)w * h * 2);
+	for (size_t p = 0; p < (size_t)w * h; p++) {
+		raw[2 * p] = planar[p];
+		raw[2 * p + 1] = planar[(size_t)w * h + p];
+	}
+	bool ok = std::fwrite(&magic, 4, 1, f) == 1 && std::fwrite(wh, 4, 2, f) == 2 &&
+	          std::fwrite(raw.data(), sizeof(float), raw.size(), f) == raw.size();
+	return std::fclose(f) == 0 && ok;
+}
+
+uint32_t crc32(const unsigned char *p, size_t n, uint32_t c = 0xffffffffu)
+{
+	for (size_t i = 0; i < n; i++) {
+		c ^= p[i];
+		for (int k = 0; k < 8; k++) c = (c >> 1) ^ (0xedb88320u & (0u - (c & 1u)));
+	}
+	return c;
+}
+
+void put32(std::vector<unsigned char> &v, uint32_t x)
+{
+	for (int s = 24; s >= 0; s -= 8) v.push_back((unsigned char)(x >> s));
+}
+
+bool write_png(const char *path, const float *planar, int w, int h, int c)
+{
+	// scanlines: filter byte 0, then 8-bit samples
+	const int cc = c == 3 ? 3 : 1;
+	std::vector<unsigned char> raw;
+	raw.reserve((size_t)h * (w * cc + 1));
+	for (int y = 0; y < h; y++) {
+		raw.push_back(0);
+		for (int x = 0; x < w; x++)
+			for (int k = 0; k < cc; k++) {
+				float v = std::round(planar[((size_t)k * h + y) * w + x]);
+				v = v < 0.f ? 0.f : (v > 255.f ? 255.f : v);
+				raw.push_back((unsigned char)v);
+			}
+	}
+	// zlib stream of stored blocks
+	std::vector<unsigned char> z = {0x78, 0x01};
+	uint32_t a = 1, b = 0;
+	for (unsigned char ch : raw) {
+		a = (a + ch) % 65521u;
+		b = (b + a) % 65521u;
+	}
+	for (size_t o = 0; o < raw.size() || raw.empty();) {
+		const size_t n = std::min<size_t>(65535, raw.size() - o);
+		const bool last = o + n == raw.size();
+		z.push_back(last ? 1 : 0);
+		z.push_back((unsigned char)(n & 0xff));
+		z.push_back((unsigned char)(n >> 8));
+		z.push_back((unsigned char)(~n & 0xff));
+		z.push_back((unsigned char)((~n >> 8) & 0xff));
+		z.insert(z.end(), raw.begin() + o, raw.begin() + o + n);
+		o += n;
+		if (last) break;
+	}
+	put32(z, (b << 16) | a);
+	std::vector<unsigned char> png = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
+	auto chunk = [&png](const char *type, const std::vector<unsigned char> &data) {
+		put32(png, (uint32_t)data.size());
+		std::vector<unsigned char> td(type, type + 4);
+		td.insert(td.end(), data.begin(), data.end());
+		png.insert(png.end(), td.begin(), td.end());
+		put32(png, crc32(td.data(), td.size()) ^ 0xffffffffu);
+	};
+	std::vector<unsigned char> ihdr;
+	put32(ihdr, (uint32_t)w);
+	put32(ihdr, (uint32_t)h);
+	ihdr.push_back(8);
+	ihdr.push_back(cc == 3 ? 2 : 0);
+	ihdr.push_back(0);
+	ihdr.push_back(0);
+	ihdr.push_back(0);
+	chunk("IHDR", ihdr);
+	chunk("IDAT", z);
+	chunk("IEND", {});
+	FILE *f = std::fopen(path, "wb");
+	if (!f) return false;
+	const bool ok = std::fwrite(png.data(), 1, png.size(), f) == png.size();
+	return std::fclose(f) == 0 && ok;
+}
+
+bool read_frame(const char *path, std::vector<float> &out, int &w, int &h, int &c)
+{
+	const std::string p(path);
+	bool ok = ends_with(p, ".flo") ? read_flo(path, out, w, h, c) : read_pfm(path, out, w, h, c);
+	if (ok && c == 3) {   // equal channels: grey (lib_image.cpp:66-73)
+		const size_t wh = (size_t)w * h;
+		size_t k = 0;
+		while (k < wh && out[k] == out[wh + k] && out[k] == out[2 * wh + k]) k++;
+		if (k == wh) {
+			out.resize(wh);
+			c = 1;
+		}
+	}
+	return ok;
+}
+
+bool write_frame(const char *path, const float *planar, int w, int h, int c)
+{
+	const std::string p(path);
+	if (ends_with(p, ".flo")) return c == 2 && write_flo(path, planar, w, h);
+	if (ends_with(p, ".png")) return write_png(path, planar, w, h, c);
+	return write_pfm(path, planar, w, h, c);
+}
+
+struct Video {
+	std::vector<float> data;
+	unsigned w = 0, h = 0, c = 0, f = 0;
+};
+
+// Video<float>::loadVideo (lib_videot.cpp:30-89)
+bool load_video(const std::string &pattern, unsigned first, unsigned last, unsigned step, Video &v,
+                std::string &err)
+{
+	char name[1024];
+	std::snprintf(name, sizeof name, pattern.c_str(), first);
+	std::vector<float> frame;
+	int w, h, c;
+	if (!read_frame(name, frame, w, h, c)) {
+		err = "Video<T>::loadVideo: loading of " + std::string(name) + " failed";
+		return false;
+	}
+	v.w = w;
+	v.h = h;
+	v.c = c;
+	v.f = (last - first + 1) / step;
+	v.data.assign((size_t)v.w * v.h * v.c * v.f, 0.f);
+	size_t o = 0;
+	std::copy(frame.begin(), frame.end(), v.data.begin());
+	o += frame.size();
+	for (unsigned t = first + step; t <= last; t += step) {
+		std::snprintf(name, sizeof name, pattern.c_str(), t);
+		if (!read_frame(name, frame, w, h, c)) {
+			err = "Video<T>::loadVideo: loading of " + std::string(name) + " failed";
+			return false;
+		}
+		if ((unsigned)w != v.w || (unsigned)h != v.h || (unsigned)c != v.c) {
+			err = "Video<T>::loadVideo: size of " + std::string(name) + " does not match video size";
+			return false;
+		}
+		if (o + frame.size() > v.data.size()) v.data.resize(o + frame.size());
+		std::copy(frame.begin(), frame.end(), v.data.begin() + o);
+		o += frame.size();
+	}
+	return true;
+}
+
+// Video<float>::saveVideo (lib_videot.cpp:91-126)
+bool save_video(const std::string &pattern, unsigned first, unsigned step, const Video &v, std::string &err)
+{
+	const size_t whc = (size_t)v.w * v.h * v.c;
+	for (unsigned k = 0; k < v.f; k++) {
+		char name[1024];
+		std::snprintf(name, sizeof name, pattern.c_str(), first + k * step);
+		if (!write_frame(name, v.data.data() + k * whc, v.w, v.h, v.c)) {
+			err = "Video<T>::saveVideo: writing of " + std::string(name) + " failed";
+			return false;
+		}
+	}
+	return true;
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+	Args a{argc, argv};
+	for (int i = 1; i < argc; i++)
+		if (!std::strcmp(argv[i], "-h") || !std::strcmp(argv[i], "--help")) a.help = true;
+	if (a.help) {
+		std::printf("%s : BM4D-OF video denoising (GB300)\n", argv[0]);
+		std::printf(" NOTE: Input (<) and output (>) sequences are specified by their paths in printf format.\n");
+	}
+	const std::string input_path = a.str("-i", "", "< input sequence");
+	const std::string inbsc_path = a.str("-b", "", "< input basic sequence");
+	const std::string final_path = a.str("-deno", "deno_%03d.png", "> denoised sequence");
+	const std::string basic_path = a.str("-bsic", "bsic_%03d.png", "> basic denoised sequence");
+	const unsigned first_frame = a.i("-f", 0, "first frame");
+	const unsigned last_frame = a.i("-l", 0, "last frame");
+	const unsigned frame_step = a.i("-s", 1, "frame step");
+	const std::string fflow_path = a.str("-fof", "", "< input forward  optical flow");
+	const std::string bflow_path = a.str("-bof", "", "< input backward optical flow");
+	const float sigma = a.f("-sigma", 0.f, "< standard deviation of the noise");
+	const bool verbose = a.i("-verbose", 1, "< verbose output") != 0;
+	const bool order_inv = a.i("-order-inv", 0, "< invariance to patch order in stack") != 0;
+	const unsigned print_prms = (unsigned)a.i("-print-prms", 0, "< prints parameters for given channels");
+	const int time_search1 = a.i("-wt1", 0, "< search window temporal radius, step 1");
+	const int time_search2 = a.i("-wt2", 0, "< search window temporal radius, step 2");
+	const int space_search1 = a.i("-wx1", -1, "< search window spatial radius, step 1");
+	const int space_search2 = a.i("-wx2", -1, "< search window spatial radius, step 2");
+	const int patch_sizex1 = a.i("-px1", -1, "< spatial patch size, step 1");
+	const int patch_sizex2 = a.i("-px2", -1, "< spatial patch size, step 2");
+	const int patch_sizet1 = a.i("-pt1", 1, "< temporal patch size, step 1");
+	const int patch_sizet2 = a.i("-pt2", 1, "< temporal patch size, step 2");
+	const int num_patches1 = a.i("-np1", -1, "< number of similar patches, step 1");
+	const int num_patches2 = a.i("-np2", -1, "< number of similar patches, step 2");
+	(void)a.f("-t1", -1.f, "< step 1 distance threshold");   // applies only to the VBM3D search build
+	(void)a.f("-t2", -1.f, "< step 2 distance threshold");
+	const float beta1 = a.f("-b1", -1.f, "< noise correction factor beta, step 1");
+	const float beta2 = a.f("-b2", -1.f, "< noise correction factor beta, step 2");
+	const float beta_mean1 = a.f("-bm1", -1.f, "< noise correction factor beta for mean, step 1");
+	const float beta_mean2 = a.f("-bm2", -1.f, "< noise correction factor beta for mean, step 2");
+	const bool no_paste1 = a.i("-no-paste1", 0, "< disable paste trick, step 1") != 0;
+	const bool no_paste2 = a.i("-no-paste2", 0, "< disable paste trick, step 2") != 0;
+	const bool no_step1 = a.i("-no-step1", 0, "< disable patch skipping, step 1") != 0;
+	const bool no_step2 = a.i("-no-step2", 0, "< disable patch skipping, step 2") != 0;
+	const bool agg_win1 = a.i("-agg-win1", 0, "< aggregation window, step 1") != 0;
+	const bool agg_win2 = a.i("-agg-win2", 0, "< aggregation window, step 2") != 0;
+	const unsigned nparts = (unsigned)a.i("-nparts", 2, "< spatial tiles (the reference: 2 x OpenMP threads)");
+	const int device = a.i("-device", 0, "< CUDA device");
+	const bool mixed = a.i("-mixed", 0, "< FP16 tensor-core distance pre-screen") != 0;
+	(void)time_search1;
+	(void)time_search2;
+	if (a.help) return EXIT_SUCCESS;
+
+	// checks of main_vnlb.cpp:89-127
+	if (input_path.empty())
+		return std::fprintf(stderr, "%s: no input sequence.\nTry `%s --help' for more information.\n", argv[0],
+		                    argv[0]),
+		       EXIT_FAILURE;
+	if (patch_sizex1 == 0 && patch_sizex2 > 0 && inbsc_path.empty())
+		return std::fprintf(stderr,
+		                    "%s: if px1 = 0 and px2 > 0, a basic sequence path must be given.\n"
+		                    "Try `%s --help' for more information.\n",
+		                    argv[0], argv[0]),
+		       EXIT_FAILURE;
+	if ((patch_sizex1 < 0 && patch_sizex1 != -1) || (patch_sizex2 < 0 && patch_sizex2 != -1) ||
+	    (patch_sizet1 < 0 || patch_sizet2 < 0))
+		return std::fprintf(stderr, "%s: px1, px2, pt1 and pt2 cannot be negative.\n"
+		                            "Try `%s --help' for more information.\n", argv[0], argv[0]),
+		       EXIT_FAILURE;
+	if ((num_patches1 < 0 && num_patches1 != -1) || (num_patches2 < 0 && num_patches2 != -1))
+		return std::fprintf(stderr, "%s: np1 and np2 cannot be negative.\n"
+		                            "Try `%s --help' for more information.\n", argv[0], argv[0]),
+		       EXIT_FAILURE;
+	if ((space_search1 < 0 && space_search1 != -1) || (space_search2 < 0 && space_search2 != -1) ||
+	    (time_search1 < 0 || time_search2 < 0))
+		return std::fprintf(stderr, "%s: wx1, wx2, wt1 and wt2 cannot be negative.\n"
+		                            "Try `%s --help' for more information.\n", argv[0], argv[0]),
+		       EXIT_FAILURE;
+	if (patch_sizex1 > 0 && !inbsc_path.empty())
+		std::fprintf(stderr, "\x1b[33;1mWarning:\x1b[0m a basic sequence path ignored since px1 > 0.\n");
+	if (fflow_path.empty() != bflow_path.empty())
+		return std::fprintf(stderr, "Only one oflow path provided.\nTry `%s --help' for more information.\n",
+		                    argv[0]),
+		       EXIT_FAILURE;
+	if (patch_sizex1 == 0 && patch_sizex2 == 0)
+		return std::fprintf(stderr, "Given patch sizes for both steps are 0. Nothing to do.\n"), EXIT_FAILURE;
+
+	const bool deno_only = patch_sizex1 == 0 && patch_sizex2 != 0;
+	const bool use_oflow = !fflow_path.empty() && (last_frame - first_frame > frame_step);
+
+	Video noisy, basic, fflow, bflow;
+	std::string err;
+	bm4dof_video_size sz = {0, 0, 0, 0};
+	if (print_prms) {
+		sz.channels = print_prms;
+	} else {
+		if (!load_video(input_path, first_frame, last_frame, frame_step, noisy, err))
+			return std::fprintf(stderr, "%s\n", err.c_str()), EXIT_FAILURE;
+		if (deno_only && !load_video(inbsc_path, first_frame, last_frame, frame_step, basic, err))
+			return std::fprintf(stderr, "%s\n", err.c_str()), EXIT_FAILURE;
+		if (use_oflow && (!load_video(fflow_path, first_frame, last_frame, frame_step, fflow, err) ||
+		                  !load_video(bflow_path, first_frame, last_frame, frame_step, bflow, err)))
+			return std::fprintf(stderr, "%s\n", err.c_str()), EXIT_FAILURE;
+		sz.width = noisy.w;
+		sz.height = noisy.h;
+		sz.frames = noisy.f;
+		sz.channels = noisy.c;
+		if (verbose) std::printf("Running BM4D-OF on the noisy video\n");
+	}
+
+	// parameters (main_vnlb.cpp:206-246)
+	bm4dof_params p1, p2;
+	bm4dof_initialize_params(&p1, 1, sigma, &sz, print_prms ? verbose : verbose);
+	bm4dof_initialize_params(&p2, 2, sigma, &sz, verbose);
+	if (space_search1 >= 0) bm4dof_set_size_search_window(&p1, (unsigned)space_search1);
+	if (space_search2 >= 0) bm4dof_set_size_search_window(&p2, (unsigned)space_search2);
+	if (patch_sizex1 >= 0) bm4dof_set_size_patch(&p1, &sz, (unsigned)patch_sizex1);
+	if (patch_sizex2 >= 0) bm4dof_set_size_patch(&p2, &sz, (unsigned)patch_sizex2);
+	if (num_patches1 >= 0) bm4dof_set_n_similar_patches(&p1, (unsigned)num_patches1);
+	if (num_patches2 >= 0) bm4dof_set_n_similar_patches(&p2, (unsigned)num_patches2);
+	if (beta1 >= 0) p1.beta = beta1;
+	if (beta2 >= 0) p2.beta = beta2;
+	if (beta1 >= 0) p1.betaMean = beta1;
+	if (beta2 >= 0) p2.betaMean = beta2;
+	if (beta_mean1 >= 0) p1.betaMean = beta_mean1;
+	if (beta_mean2 >= 0) p2.betaMean = beta_mean2;
+	if (patch_sizet1 >= 0) p1.sizePatchTime = patch_sizet1;
+	if (patch_sizet2 >= 0) p2.sizePatchTime = patch_sizet2;
+	if (agg_win1) p1.agg_window = 1;
+	if (agg_win2) p2.agg_window = 1;
+	if (no_paste1) p1.doPasteBoost = 0;
+	if (no_paste2) p2.doPasteBoost = 0;
+	if (no_step1) p1.offSet = 1;
+	if (no_step2) p2.offSet = 1;
+	if (order_inv) p1.orderInvariance = p2.orderInvariance = 1;
+	if (print_prms) {
+		bm4dof_print_params(&p1);
+		bm4dof_print_params(&p2);
+		return EXIT_SUCCESS;
+	}
+
+	bm4dof_ctx *ctx = nullptr;
+	if (bm4dof_create(&ctx, device) != BM4DOF_OK)
+		return std::fprintf(stderr, "%s\n", bm4dof_last_error()), EXIT_FAILURE;
+	Video fin = noisy;
+	if (!deno_only) basic = noisy;
+	float ratios[2] = {0.f, 0.f};
+	const bm4dof_status s =
+	    bm4dof_run(ctx, noisy.data.data(), use_oflow ? fflow.data.data() : nullptr,
+	               use_oflow ? bflow.data.data() : nullptr, noisy.w, noisy.h, noisy.c, noisy.f, basic.data.data(),
+	               fin.data.data(), &p1, &p2, nparts, mixed ? BM4DOF_MIXED_PRECISION : 0u, ratios);
+	bm4dof_destroy(ctx);
+	if (s != BM4DOF_OK) return std::fprintf(stderr, "%s\n", bm4dof_last_error()), EXIT_FAILURE;
+	if (verbose)
+		std::printf("Done. Processed %5.2f%% of possible patch groups in 1st step, and\n"
+		            "%5.2f%% in 2nd step.\n", ratios[0], ratios[1]);
+	if (verbose) std::printf("\nSaving output sequences\n");
+	if (p2.sizePatch && !save_video(final_path, first_frame, frame_step, fin, err))
+		return std::fprintf(stderr, "%s\n", err.c_str()), EXIT_FAILURE;
+	if (!save_video(basic_path, first_frame, frame_step, basic, err))
+		return std::fprintf(stderr, "%s\n", err.c_str()), EXIT_FAILURE;
+	return EXIT_SUCCESS;
+}

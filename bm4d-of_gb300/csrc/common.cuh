@@ -48,6 +48,10 @@ struct StepParams {               // resolved parameters of one step
 	int chn_search;               // channels compared by the distance
 	float sigma, beta, tau2;      // tau2 = tau*tau*px*px*pt (nldct.cpp:1158)
 	int use_flow;
+	float beta1;                  // learned form: hard threshold of the non-mean Haar rows
+	int search_ctas;              // exact search: CTAs per SM (4 or 6; 0 = default)
+	float beta_mean;              // betaMean (order-invariant filtering)
+	int order_inv;                // orderInvariance
 };
 
 // Locate the tile owning global group g (tiles are few: linear scan).

@@ -63,18 +63,41 @@ __device__ __forceinline__ void haar_inverse(float (&z)[NS], float is2)
 		}
 }
 
+// std::max(a, 0.f) as libstdc++ evaluates it ((a < 0) ? 0 : a, NaN kept)
+__device__ __forceinline__ float max0(float a) { return a < 0.f ? 0.f : a; }
+
 // One transform coefficient k of one channel: Haar over the NS members,
 // shrinkage, inverse Haar.  Returns the number of kept coefficients (step 1).
+// With order invariance (nldct.cpp:1865-1900, 2101-2122) one Wiener gain
+// serves the mean row and one all other rows; the coefficient's share of the
+// group weight, w0^2 + (NS-1) wi^2, goes to *contrib.
 template <int NS, int STEP>
 __device__ int shrink_column(float *zcol, const float *ycol, float *w2col, int k, float bs2,
-                             float is2)
+                             float is2, bool oinv, float sigma2, float bm2, float *contrib)
 {
 	float z[NS];
 #pragma unroll
 	for (int n = 0; n < NS; n++) z[n] = zcol[n];
 	haar_forward<NS>(z, is2);
 	int kept = 0;
-	if (STEP == 1) {
+	if (oinv) {
+		float y[NS];
+#pragma unroll
+		for (int n = 0; n < NS; n++) y[n] = STEP == 1 ? z[n] : ycol[n];
+		if (STEP == 2) haar_forward<NS>(y, is2);
+		float vi = 0.f;
+#pragma unroll
+		for (int n = 1; n < NS; n++) vi = __fadd_rn(vi, __fmul_rn(y[n], y[n]));
+		vi = __fdiv_rn(vi, (float)(NS - 1));
+		const float v0 = STEP == 1 ? max0(__fsub_rn(__fmul_rn(y[0], y[0]), sigma2)) : __fmul_rn(y[0], y[0]);
+		const float w0 = __fdiv_rn(v0, __fadd_rn(v0, bm2));
+		z[0] = __fmul_rn(z[0], w0);
+		if (STEP == 1) vi = max0(__fsub_rn(vi, sigma2));
+		const float wi = __fdiv_rn(vi, __fadd_rn(vi, bs2));
+#pragma unroll
+		for (int n = 1; n < NS; n++) z[n] = __fmul_rn(z[n], wi);
+		*contrib = __fadd_rn(__fmul_rn(w0, w0), __fmul_rn(__fmul_rn((float)(NS - 1), wi), wi));
+	} else if (STEP == 1) {
 #pragma unroll
 		for (int n = 0; n < NS; n++) {
 			if (__fmul_rn(z[n], z[n]) > bs2 || (k == 0 && n == 0)) kept++;
@@ -101,16 +124,18 @@ __device__ int shrink_column(float *zcol, const float *ycol, float *w2col, int k
 
 template <int STEP>
 __device__ int shrink_dispatch(int ns, float *zcol, const float *ycol, float *w2col, int k,
-                               float bs2, float is2)
+                               float bs2, float is2, bool oinv, float sigma2, float bm2, float *contrib)
 {
+#define SHRINK(N) shrink_column<N, STEP>(zcol, ycol, w2col, k, bs2, is2, oinv, sigma2, bm2, contrib)
 	switch (ns) {
-	case 1: return shrink_column<1, STEP>(zcol, ycol, w2col, k, bs2, is2);
-	case 2: return shrink_column<2, STEP>(zcol, ycol, w2col, k, bs2, is2);
-	case 4: return shrink_column<4, STEP>(zcol, ycol, w2col, k, bs2, is2);
-	case 8: return shrink_column<8, STEP>(zcol, ycol, w2col, k, bs2, is2);
-	case 16: return shrink_column<16, STEP>(zcol, ycol, w2col, k, bs2, is2);
-	default: return shrink_column<32, STEP>(zcol, ycol, w2col, k, bs2, is2);
+	case 1: return SHRINK(1);
+	case 2: return SHRINK(2);
+	case 4: return SHRINK(4);
+	case 8: return SHRINK(8);
+	case 16: return SHRINK(16);
+	default: return SHRINK(32);
 	}
+#undef SHRINK
 }
 
 // out(n, q) = sum_r in(n, r) * M[r*spc + q], r increasing, for a block of 4
@@ -130,8 +155,11 @@ __device__ __forceinline__ void product4(const float *in, const float *M, float 
 	*reinterpret_cast<float4 *>(out + q * nsp + n0) = make_float4(a0, a1, a2, a3);
 }
 
-template <int STEP>
-__global__ void __launch_bounds__(kFilterThreads)
+// PX, PT, CC: patch size, patch frames and channels when known at compile
+// time (0: taken from sp), so that the index arithmetic of the per-element
+// loops folds into shifts and multiplies.
+template <int STEP, int PX, int PT, int CC>
+__global__ void __launch_bounds__(kFilterThreads, STEP == 2 ? 3 : 4)
 filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, int ntiles,
                     StepParams sp, const float *__restrict__ basis, const float *__restrict__ binv,
                     const float *__restrict__ win, long long g_begin, long long g_end,
@@ -140,7 +168,8 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
                     float *__restrict__ wslot, float *__restrict__ wgroup, uint8_t *__restrict__ eq)
 {
 	extern __shared__ __align__(16) float sm[];
-	const int spc = sp.spc, C = sp.C, np = sp.np;
+	const int px = PX ? PX : sp.px, pt = PT ? PT : sp.pt, C = CC ? CC : sp.C;
+	const int spc = px * px * pt, np = sp.np;
 	const int nsp = nsp_of(np);
 	const int tile_f = C * spc * nsp;          // floats of one group tile (all channels)
 	const int bsz = ((spc * spc + 3) / 4) * 4; // basis sizes padded: the group tiles
@@ -167,6 +196,9 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
 	const float sigma2 = __fmul_rn(sp.sigma, sp.sigma);
 	const float bsig = __fmul_rn(sp.beta, sp.sigma);
 	const float bs2 = __fmul_rn(bsig, bsig);
+	const float bmsig = __fmul_rn(sp.beta_mean, sp.sigma);
+	const float bm2 = __fmul_rn(bmsig, bmsig);
+	const bool oinv = sp.order_inv != 0;
 	const float is2 = (float)(1.0 / sqrt(2.0));
 
 	for (long long g = g_begin + blockIdx.x; g < g_end; g += gridDim.x) {
@@ -196,7 +228,7 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
 		for (int it = tid; it < ns * per; it += blockDim.x) {
 			const int n = it / per, r = it % per;
 			const int c = r / spc, p = r % spc;
-			const int ht = p / (sp.px * sp.px), hy = (p / sp.px) % sp.px, hx = p % sp.px;
+			const int ht = p / (px * px), hy = (p / px) % px, hx = p % px;
 			const size_t a = noisy.at(T.ox + s_mx[n] + hx, T.oy + s_my[n] + hy, s_mt[n] + ht, c);
 			Gn[(c * spc + p) * nsp + n] = __ldg(noisy.p + a);
 			if (STEP == 2) Gb[(c * spc + p) * nsp + n] = __ldg(basic.p + a);
@@ -239,7 +271,8 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
 		int kept = 0;
 		for (int it = tid; it < C * spc; it += blockDim.x) {
 			const int k = it % spc;
-			kept += shrink_dispatch<STEP>(ns, Zn + it * nsp, Zb + it * nsp, Gb + it * ns, k, bs2, is2);
+			kept += shrink_dispatch<STEP>(ns, Zn + it * nsp, Zb + it * nsp, Gb + it * ns, k, bs2, is2, oinv,
+			                              sigma2, bm2, Gb + it);
 		}
 		if (STEP == 1 && kept) atomicAdd(&s_kept, kept);
 		__syncthreads();
@@ -248,7 +281,12 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
 		// while one lane forms the group weight
 		if (tid < 32) {
 			if (tid == 0) {
-				if (STEP == 1) {
+				if (oinv) {
+					// float sum of the coefficients' shares in (c, k) order
+					float v = 0.f;
+					for (int i = 0; i < C * spc; i++) v = __fadd_rn(v, Gb[i]);
+					s_w = STEP == 1 ? __fdiv_rn(__fdiv_rn(1.f, sigma2), v) : (float)(1.0 / (double)sigma2 / (double)v);
+				} else if (STEP == 1) {
 					s_w = __fdiv_rn(__fdiv_rn(1.f, sigma2), (float)s_kept);
 				} else {
 					float v = 0.f;   // sum of w^2 in the reference's (c, k, n) order
@@ -319,6 +357,29 @@ size_t filter_smem_bytes(const StepParams &sp)
 	return sizeof(float) * (2 * bsz + ((sp.spc + 3) / 4) * 4 + 4 * tile_f);
 }
 
+namespace {
+
+template <int STEP, int PX, int PT, int CC>
+cudaError_t launch_exact(int blocks, size_t smem, cudaStream_t st, const Image &noisy, const Image &basic,
+                         const Tile *tiles, int ntiles, const StepParams &sp, const float *basis, const float *binv,
+                         const float *win, long long g_begin, long long g_end, const uint8_t *nsimp,
+                         const uint32_t *idx, const uint8_t *alive, float *vals, float *wslot, float *wgroup,
+                         uint8_t *eq)
+{
+	auto kern = filter_exact_kernel<STEP, PX, PT, CC>;
+	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess) return e;
+	kern<<<blocks, kFilterThreads, smem, st>>>(noisy, basic, tiles, ntiles, sp, basis, binv, win, g_begin, g_end,
+	                                          nsimp, idx, alive, vals, wslot, wgroup, eq);
+	return cudaGetLastError();
+}
+
+#define FILTER_ARGS                                                                                   \
+	blocks, smem, st, noisy, basic, tiles, ntiles, sp, basis, binv, win, g_begin, g_end, nsimp, idx, alive, \
+	    vals, wslot, wgroup, eq
+
+}  // namespace
+
 cudaError_t launch_filter(const Image &noisy, const Image &basic, const Tile *tiles, int ntiles,
                           const StepParams &sp, const float *basis, const float *binv,
                           const float *win, long long g_begin, long long g_end,
@@ -331,19 +392,13 @@ cudaError_t launch_filter(const Image &noisy, const Image &basic, const Tile *ti
 	const long long n = g_end - g_begin;
 	const int blocks = (int)(n < (long long)nsm * 8 ? n : (long long)nsm * 8);
 	cudaError_t e;
-	if (sp.step1) {
-		e = cudaFuncSetAttribute(filter_exact_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		if (e != cudaSuccess) return e;
-		filter_exact_kernel<1><<<blocks, kFilterThreads, smem, st>>>(noisy, basic, tiles, ntiles, sp, basis, binv, win,
-		                                                             g_begin, g_end, nsimp, idx, alive, vals,
-		                                                             wslot, wgroup, eq);
-	} else {
-		e = cudaFuncSetAttribute(filter_exact_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		if (e != cudaSuccess) return e;
-		filter_exact_kernel<2><<<blocks, kFilterThreads, smem, st>>>(noisy, basic, tiles, ntiles, sp, basis, binv, win,
-		                                                             g_begin, g_end, nsimp, idx, alive, vals,
-		                                                             wslot, wgroup, eq);
-	}
+	if (sp.C == 1 && sp.px == 4 && sp.pt == 4)
+		e = sp.step1 ? launch_exact<1, 4, 4, 1>(FILTER_ARGS) : launch_exact<2, 4, 4, 1>(FILTER_ARGS);
+	else if (sp.C == 1 && sp.px == 8 && sp.pt == 1)
+		e = sp.step1 ? launch_exact<1, 8, 1, 1>(FILTER_ARGS) : launch_exact<2, 8, 1, 1>(FILTER_ARGS);
+	else
+		e = sp.step1 ? launch_exact<1, 0, 0, 0>(FILTER_ARGS) : launch_exact<2, 0, 0, 0>(FILTER_ARGS);
+	if (e != cudaSuccess) return e;
 	e = cudaGetLastError();
 	if (e != cudaSuccess) return e;
 	const int fb = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);

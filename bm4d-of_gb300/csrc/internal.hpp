@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -53,6 +54,9 @@ cudaError_t launch_kill_edges(const Tile *tiles, int ntiles, const int *grid, co
                               cudaStream_t st);
 cudaError_t launch_kill_iteration(const unsigned long long *edges, unsigned n, uint8_t *alive,
                                   uint8_t *killed, unsigned *changed, cudaStream_t st);
+// Switch-offs resolved on the device in one launch (no host round trip).
+cudaError_t launch_kill_fixpoint(const unsigned long long *edges, const unsigned *nedges, unsigned cap,
+                                 uint8_t *alive, uint8_t *killed, cudaStream_t st);
 cudaError_t launch_count_alive(const Tile *tiles, int ntiles, long long G, const uint8_t *alive,
                                unsigned *counts, cudaStream_t st);
 cudaError_t exclusive_scan(unsigned *data, size_t n, unsigned *scratch, cudaStream_t st);
@@ -70,5 +74,57 @@ cudaError_t launch_color(const Image &in, const Image &out, int forward, cudaStr
 cudaError_t launch_finalize(const Tile *tiles, int nW, int wTmp, int hTmp, const StepParams &sp,
                             const Image &noisy, const float *acc, const float *wacc,
                             const Image &out, int inverse_color, cudaStream_t st);
+
+// mlp.cu -- gain network 65 -> 256 -> 256 -> 64 (W1 padded to 80 inputs)
+constexpr int kMlpIn = 65, kMlpInPad = 80, kMlpHid = 256, kMlpOutN = 64;
+constexpr int kMlpOffW1 = 0, kMlpOffB1 = kMlpInPad * kMlpHid, kMlpOffW2 = kMlpOffB1 + kMlpHid,
+              kMlpOffB2 = kMlpOffW2 + kMlpHid * kMlpHid, kMlpOffW3 = kMlpOffB2 + kMlpHid,
+              kMlpOffB3 = kMlpOffW3 + kMlpHid * kMlpOutN, kMlpMasterSize = kMlpOffB3 + kMlpOutN;
+constexpr int kMlpPublicSize = kMlpMasterSize - (kMlpInPad - kMlpIn) * kMlpHid;
+constexpr int kMlpWtSize = kMlpHid * kMlpInPad + kMlpHid * kMlpHid + kMlpOutN * kMlpHid;
+struct MlpWeights {
+	const __nv_bfloat16 *wt1, *wt2, *wt3;   // transposed [out][in]
+	const float *b1, *b2, *b3;
+};
+MlpWeights mlp_weights(const uint16_t *wt, const float *master);
+void mlp_public_to_master(const float *pub, float *master);
+void mlp_master_to_public(const float *master, float *pub);
+cudaError_t launch_pack_weights(const float *master, uint16_t *wt, cudaStream_t st);
+cudaError_t launch_mlp_forward(const uint16_t *X, long long n, const MlpWeights &w, float *out, int nsm,
+                               cudaStream_t st);
+
+// learned.cu
+enum { kLearnedFeatures = 0, kLearnedApply = 1, kLearnedSamples = 2 };
+struct LearnedArgs {
+	Image noisy, basic;
+	const Tile *tiles;
+	int ntiles;
+	long long ga, gb;                    // group range (rows are g - ga)
+	const uint8_t *nsimp, *alive;
+	const uint32_t *idx;
+	const float *basis, *binv, *win;
+	__nv_bfloat16 *feat;                 // features: [rows][80]
+	const float *gains;                  // apply: [rows][64], or null (no network)
+	float *vals, *wslot;                 // apply: aggregation terms and weights
+	float kappa;                         // apply: residual-variance fallback threshold
+	unsigned *nfallback;
+	float *sfeat, *starget;              // samples: [G][65], [G][64]
+	uint8_t *svalid;                     // samples: [G]
+};
+bool learned_supported(const StepParams &sp);
+cudaError_t launch_learned(int mode, const LearnedArgs &a, const StepParams &sp, int nsm, cudaStream_t st);
+
+// tvl1.cu -- TV-L1 optical flow, batched over frame pairs
+struct Tvl1Params {
+	float tau, lambda, theta;
+	int nscales, fscale;
+	float zfactor;
+	int warps;
+	float epsilon;
+};
+int tvl1_scales(int nx, int ny, int nscales, float zfactor);
+size_t tvl1_workspace_floats(int nx, int ny, int npairs, int nscales, float zfactor);
+cudaError_t tvl1_flow(const float *I0, const float *I1, int nx, int ny, int npairs, const Tvl1Params &p, float *u,
+                      float *v, float *ws, int *iws, int nsm, cudaStream_t st, std::string &why);
 
 }  // namespace bm4dof

@@ -16,18 +16,17 @@
 //   traj_kernel    one thread per group: the flow-chained search centres of
 //                  every frame of its temporal range (a short dependent chain
 //                  of flow reads, kept out of the distance kernel);
-//   search_kernel  one CTA per group at a time: each candidate frame's window
-//                  (plus patch halo, all patch frames) is copied into shared
-//                  memory by a TMA tensor load, double buffered behind an
-//                  mbarrier; threads compute register-tiled strips of SW
-//                  horizontally adjacent candidates with the reference patch
-//                  held in registers; warp 0 then runs the heap selection with
-//                  ballots so that only candidates below the current heap top
-//                  are handled one at a time.  The next group's first windows
-//                  are requested before the selection starts.
-#include <cuda.h>
+//   search_kernel  one CTA per group at a time: warp 0 lays out the candidate
+//                  windows; every thread computes column strips of kR
+//                  vertically adjacent candidates (lanes on consecutive
+//                  columns, window rows read through L1, the reference patch
+//                  from shared memory one patch frame at a time into
+//                  registers); the distances land in shared memory in the
+//                  reference's candidate order; the k nearest are selected by
+//                  a bound from the per-thread minima, compaction and a warp
+//                  bitonic sort, with an exact replay of the heap selection
+//                  when ties make that order ambiguous.
 #include <cuda_runtime.h>
-#include <cudaTypedefs.h>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -40,52 +39,11 @@ namespace bm4dof {
 namespace {
 
 constexpr int kThreads = 192;          // 6 warps: 567 column strips of a 21x21x9 window set in 3 rounds
-constexpr int kSW = 7;                 // candidates per thread along x (horizontal strips)
 constexpr int kR = 7;                  // candidates per thread along y (column strips)
-constexpr unsigned kWaitLimit = 1u << 24;
 
 struct FrameWin {
-	int qt, rx0, ry0, nx, ny, cbase, ibase, xoff, X0;
+	int qt, rx0, ry0, nx, ny, cbase, ibase;
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-	return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
-{
-	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
-{
-	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-	             : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
-{
-	uint32_t ok;
-	asm volatile(
-		"{\n\t.reg .pred p;\n\t"
-		"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-		"selp.u32 %0, 1, 0, p;\n\t}"
-		: "=r"(ok)
-		: "r"(smem_u32(bar)), "r"(parity)
-		: "memory");
-	return ok != 0;
-}
-
-__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y,
-                                            int c, int t)
-{
-	asm volatile(
-		"cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-		" [%0], [%1, {%3, %4, %5, %6}], [%2];" ::"r"(smem_u32(dst)),
-		"l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(c), "r"(t)
-		: "memory");
-}
 
 // libstdc++ __adjust_heap + __push_heap for a max-heap on distance ("less"
 // comparator comparaisonFirst, src/utils/utilities.cpp:35-41).
@@ -201,17 +159,17 @@ struct SearchArgs {
 	const int *grid;
 	const uint32_t *traj;
 	int nfm;
-	int BX, BY, CB;            // TMA box: x, y, channels (pt frames)
 	long long g_begin, g_end;
 	uint8_t *nsimp;
 	uint32_t *idx;
-	int *err;
 };
 
-// Window table of one group (thread 0).
+// Window table of one group, one lane per frame of the temporal range
+// (warp 0): candidate and column-strip offsets by warp prefix sums.
 __device__ void plan_group(const SearchArgs &a, const StepParams &sp, long long g, FrameWin *fw, int &nframes,
-                           int &ncand, int &nitems, int &tile, int &gx, int &gy, int &gt, int nstrip_w)
+                           int &ncand, int &nitems, int &tile, int &gx, int &gy, int &gt)
 {
+	const int lane = threadIdx.x & 31;
 	const int ti = tile_of(a.tiles, a.ntiles, g);
 	const Tile T = a.tiles[ti];
 	int x, y, t, t0, t1;
@@ -219,91 +177,40 @@ __device__ void plan_group(const SearchArgs &a, const StepParams &sp, long long 
 	temporal_range(sp, t, t0, t1);
 	const int nwt = t1 - t0 + 1;
 	const int hw = (sp.wx - 1) / 2;
-	int cb = 0, ib = 0;
-	for (int ii = 0; ii < nwt; ii++) {
-		const uint32_t c = a.traj[g * a.nfm + ii];
+	FrameWin f = {0, 0, 0, 0, 0, 0, 0};
+	int cnt = 0, items = 0;
+	if (lane < nwt) {
+		const uint32_t c = a.traj[g * a.nfm + lane];
 		const int cx = (int)(c & 0xffffu), cy = (int)(c >> 16);
 		const int shx = min(0, cx - hw) + max(0, cx + hw - T.w + sp.px);
 		const int shy = min(0, cy - hw) + max(0, cy + hw - T.h + sp.px);
 		const int rx0 = max(0, cx - hw - shx), ry0 = max(0, cy - hw - shy);
 		const int rx1 = min(T.w - sp.px, cx + hw - shx), ry1 = min(T.h - sp.px, cy + hw - shy);
-		FrameWin f;
-		f.qt = visit_frame(ii, t, t1);
+		f.qt = visit_frame(lane, t, t1);
 		f.rx0 = rx0;
 		f.ry0 = ry0;
 		f.nx = max(0, rx1 - rx0 + 1);
 		f.ny = max(0, ry1 - ry0 + 1);
-		f.cbase = cb;
-		f.ibase = ib;
-		f.X0 = (T.ox + rx0) & ~3;           // TMA x coordinate: 16-byte aligned
-		f.xoff = T.ox + rx0 - f.X0;
-		cb += f.nx * f.ny;
-		ib += f.nx * ((f.ny + kR - 1) / kR);
-		fw[ii] = f;
+		cnt = f.nx * f.ny;
+		items = f.nx * ((f.ny + kR - 1) / kR);
 	}
-	nframes = nwt;
-	ncand = cb;
-	nitems = ib;
-	tile = ti;
-	gx = x;
-	gy = y;
-	gt = t;
-	(void)nstrip_w;
-}
-
-// Distances of kSW horizontally adjacent candidates.  The window rows come
-// from shared memory (STAGE: the frame's TMA box, row pitch BX) or straight
-// from the video in global memory.  REFREG: the reference patch (one channel,
-// PX*PX*PT values) lives in registers, else in shared memory.
-template <int PX, int PT, bool REFREG>
-__device__ __forceinline__ void strip_distances(const float *base, size_t rpitch, size_t cpitch, size_t tpitch,
-                                                int xs, int xmax, int chn, int px_rt, int pt_rt,
-                                                const float *ref_s,
-                                                const float (&ref_r)[(PX > 0 ? PX * PX * PT : 1)],
-                                                float acc[kSW])
-{
-	const int px = PX > 0 ? PX : px_rt;
-	const int pt = PT > 0 ? PT : pt_rt;
+	int ic = cnt, ii = items;
 #pragma unroll
-	for (int j = 0; j < kSW; j++) acc[j] = 0.f;
-	if (PX > 0) {
-		constexpr int NV = (PX > 0 ? PX : 1) + kSW - 1;
-		constexpr int SPC = (PX > 0 ? PX * PX * PT : 1);
-		for (int c = 0; c < chn; c++)
-#pragma unroll
-			for (int ht = 0; ht < (PT > 0 ? PT : 1); ht++)
-#pragma unroll
-				for (int hy = 0; hy < PX; hy++) {
-					const float *row = base + ht * tpitch + c * cpitch + hy * rpitch;
-					float v[NV];
-#pragma unroll
-					for (int j = 0; j < NV; j++) v[j] = row[min(xs + j, xmax)];
-#pragma unroll
-					for (int hx = 0; hx < PX; hx++) {
-						const int kk = (ht * PX + hy) * PX + hx;
-						const float r = REFREG ? ref_r[kk] : ref_s[c * SPC + kk];
-#pragma unroll
-						for (int j = 0; j < kSW; j++) {
-							const float d = __fsub_rn(r, v[j + hx]);
-							acc[j] = __fadd_rn(acc[j], __fmul_rn(d, d));
-						}
-					}
-				}
-	} else {
-		int k = 0;
-		for (int c = 0; c < chn; c++)
-			for (int ht = 0; ht < pt; ht++)
-				for (int hy = 0; hy < px; hy++) {
-					const float *row = base + ht * tpitch + c * cpitch + hy * rpitch;
-					for (int hx = 0; hx < px; hx++, k++) {
-						const float r = ref_s[k];
-#pragma unroll
-						for (int j = 0; j < kSW; j++) {
-							const float d = __fsub_rn(r, row[min(xs + j + hx, xmax)]);
-							acc[j] = __fadd_rn(acc[j], __fmul_rn(d, d));
-						}
-					}
-				}
+	for (int o = 1; o < 32; o <<= 1) {
+		const int uc = __shfl_up_sync(0xffffffffu, ic, o), ui = __shfl_up_sync(0xffffffffu, ii, o);
+		if (lane >= o) { ic += uc; ii += ui; }
+	}
+	f.cbase = ic - cnt;
+	f.ibase = ii - items;
+	if (lane < nwt) fw[lane] = f;
+	if (lane == 31) {
+		nframes = nwt;
+		ncand = ic;
+		nitems = ii;
+		tile = ti;
+		gx = x;
+		gy = y;
+		gt = t;
 	}
 }
 
@@ -451,7 +358,9 @@ __device__ void select_knn(const float *dist, int ncand, int K, float tmin, Sele
 // 0, channel 0).  Each image row is loaded once and feeds every candidate
 // whose patch covers it; per candidate the terms still follow the reference's
 // (c, ht, hy, hx) order.  Consecutive lanes take consecutive columns, so each
-// warp-wide load touches one or two contiguous row segments.
+// warp-wide load touches one or two contiguous row segments.  With the
+// reference patch in shared memory (ref_s, 16-byte aligned), small patches
+// take one patch frame of it at a time into registers with vector loads.
 template <int PX, int PT, bool REFREG>
 __device__ __forceinline__ void col_distances(const float *col, size_t rpitch, size_t cpitch, size_t tpitch,
                                               int ymax, int chn, int px_rt, int pt_rt, const float *ref_s,
@@ -462,29 +371,67 @@ __device__ __forceinline__ void col_distances(const float *col, size_t rpitch, s
 	if (PX > 0) {
 		constexpr int SPC = (PX > 0 ? PX * PX * PT : 1);
 		constexpr int Q = PX > 0 ? PX : 1;
-		for (int c = 0; c < chn; c++)
+		constexpr bool SLICE = !REFREG && Q * Q <= 16;   // one patch frame in registers
+		if constexpr (SLICE) {
+			// patch frames one at a time (not unrolled: bounded register use)
+			for (int c = 0; c < chn; c++)
+#pragma unroll 1
+				for (int ht = 0; ht < PT; ht++) {
+					float rs[Q * Q];
+					const float4 *rp = reinterpret_cast<const float4 *>(ref_s + c * SPC + ht * Q * Q);
 #pragma unroll
-			for (int ht = 0; ht < (PT > 0 ? PT : 1); ht++)
+					for (int q = 0; q < Q * Q / 4; q++) {
+						const float4 v4 = rp[q];
+						rs[4 * q] = v4.x;
+						rs[4 * q + 1] = v4.y;
+						rs[4 * q + 2] = v4.z;
+						rs[4 * q + 3] = v4.w;
+					}
+					const float *base = col + ht * tpitch + c * cpitch;
 #pragma unroll
-				for (int yy = 0; yy < kR + Q - 1; yy++) {
-					const float *row = col + ht * tpitch + c * cpitch + (size_t)min(yy, ymax) * rpitch;
-					float v[Q];
+					for (int yy = 0; yy < kR + Q - 1; yy++) {
+						const float *row = base + (size_t)min(yy, ymax) * rpitch;
+						float v[Q];
 #pragma unroll
-					for (int hx = 0; hx < Q; hx++) v[hx] = __ldg(row + hx);
+						for (int hx = 0; hx < Q; hx++) v[hx] = __ldg(row + hx);
 #pragma unroll
-					for (int r = 0; r < kR; r++) {
-						const int hy = yy - r;
-						if (hy >= 0 && hy < Q) {
+						for (int r = 0; r < kR; r++) {
+							const int hy = yy - r;
+							if (hy >= 0 && hy < Q) {
 #pragma unroll
-							for (int hx = 0; hx < Q; hx++) {
-								const int kk = (ht * Q + hy) * Q + hx;
-								const float rv = REFREG ? ref_r[kk] : ref_s[c * SPC + kk];
-								const float d = __fsub_rn(rv, v[hx]);
-								acc[r] = __fadd_rn(acc[r], __fmul_rn(d, d));
+								for (int hx = 0; hx < Q; hx++) {
+									const float d = __fsub_rn(rs[hy * Q + hx], v[hx]);
+									acc[r] = __fadd_rn(acc[r], __fmul_rn(d, d));
+								}
 							}
 						}
 					}
 				}
+		} else {
+			for (int c = 0; c < chn; c++)
+#pragma unroll
+				for (int ht = 0; ht < (PT > 0 ? PT : 1); ht++)
+#pragma unroll
+					for (int yy = 0; yy < kR + Q - 1; yy++) {
+						const float *row = col + ht * tpitch + c * cpitch + (size_t)min(yy, ymax) * rpitch;
+						float v[Q];
+#pragma unroll
+						for (int hx = 0; hx < Q; hx++) v[hx] = __ldg(row + hx);
+#pragma unroll
+						for (int r = 0; r < kR; r++) {
+							const int hy = yy - r;
+							if (hy >= 0 && hy < Q) {
+#pragma unroll
+								for (int hx = 0; hx < Q; hx++) {
+									const int kk = (ht * Q + hy) * Q + hx;
+									const float rv = REFREG ? ref_r[kk] : ref_s[c * SPC + kk];
+									const float d = __fsub_rn(rv, v[hx]);
+									acc[r] = __fadd_rn(acc[r], __fmul_rn(d, d));
+								}
+							}
+						}
+					}
+		}
 	} else {
 		const int px = px_rt, pt = pt_rt, spc = px * px * pt;
 		for (int c = 0; c < chn; c++)
@@ -504,18 +451,17 @@ __device__ __forceinline__ void col_distances(const float *col, size_t rpitch, s
 	}
 }
 
-// One CTA handles one group at a time: every thread computes register-tiled
-// strips of kSW candidates (window rows read through L1 from the video), then
-// the CTA selects the k nearest.  Several CTAs share an SM so that one CTA's
+// One CTA handles one group at a time: every thread computes column strips of
+// kR candidates (window rows read through L1 from the video), then the CTA
+// selects the k nearest.  Several CTAs share an SM so that one CTA's
 // selection overlaps the others' distance work.
-template <int PX, int PT, bool REFREG>
-__global__ void __launch_bounds__(kThreads)
+template <int PX, int PT, bool REFREG, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
 search_kernel(Image src, StepParams sp, SearchArgs a)
 {
 	extern __shared__ __align__(16) float smem_f[];
-	float *dist = smem_f;
-	const int ncand_max = sp.wx * sp.wx * a.nfm;
-	float *ref_s = dist + ncand_max;                            // chn * spc
+	float *ref_s = smem_f;                                      // chn * spc, 16-byte aligned
+	float *dist = smem_f + ((sp.spc * sp.chn_search + 3) & ~3);
 	__shared__ FrameWin fw[kMaxFrames];
 	__shared__ int s_nframes, s_ncand, s_nitems, s_tile, s_x, s_y, s_t;
 	__shared__ SelectShared S;
@@ -523,8 +469,7 @@ search_kernel(Image src, StepParams sp, SearchArgs a)
 	const int tid = threadIdx.x;
 	const int chn = sp.chn_search;
 	for (long long g = a.g_begin + blockIdx.x; g < a.g_end; g += gridDim.x) {
-		if (tid == 0)
-			plan_group(a, sp, g, fw, s_nframes, s_ncand, s_nitems, s_tile, s_x, s_y, s_t, 0);
+		if (tid < 32) plan_group(a, sp, g, fw, s_nframes, s_ncand, s_nitems, s_tile, s_x, s_y, s_t);
 		__syncthreads();
 		const Tile T = a.tiles[s_tile];
 		const int nframes = s_nframes;
@@ -567,19 +512,18 @@ search_kernel(Image src, StepParams sp, SearchArgs a)
 		const int ncand = s_ncand;
 		const int K = min(sp.np, ncand);
 		select_knn(dist, ncand, K, tmin, S);
-		if (tid == 0) {
-			int n = 1;
-			while (2 * n <= K && S.sd[n] < sp.tau2) n *= 2;   // nldct.cpp:1284-1289
-			a.nsimp[g] = (uint8_t)n;
-			for (int q = 0; q < n; q++) {
-				const int c = S.si[q];
-				int jj = 0;
-				while (jj + 1 < nframes && fw[jj + 1].cbase <= c) jj++;
-				const FrameWin &f = fw[jj];
-				const int rl = c - f.cbase;
-				const int qy = f.ry0 + rl / f.nx, qx = f.rx0 + rl % f.nx;
-				a.idx[g * sp.np + q] = (uint32_t)(((long long)f.qt * T.h + qy) * T.w + qx);
-			}
+		// tau rule (nldct.cpp:1284-1289), then one thread per kept neighbour
+		int n = 1;
+		while (2 * n <= K && S.sd[n] < sp.tau2) n *= 2;
+		if (tid == 0) a.nsimp[g] = (uint8_t)n;
+		if (tid < n) {
+			const int c = S.si[tid];
+			int jj = 0;
+			while (jj + 1 < nframes && fw[jj + 1].cbase <= c) jj++;
+			const FrameWin &f = fw[jj];
+			const int rl = c - f.cbase;
+			const int qy = f.ry0 + rl / f.nx, qx = f.rx0 + rl % f.nx;
+			a.idx[g * sp.np + tid] = (uint32_t)(((long long)f.qt * T.h + qy) * T.w + qx);
 		}
 		__syncthreads();
 	}
@@ -600,33 +544,19 @@ __global__ void search_single_kernel(const Tile *__restrict__ tiles, int ntiles,
 	}
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
-{
-	static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-	if (!fn) {
-		void *p = nullptr;
-		cudaDriverEntryPointQueryResult q;
-		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-		        cudaSuccess &&
-		    q == cudaDriverEntryPointSuccess)
-			fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-	}
-	return fn;
-}
-
-template <int PX, int PT, bool REFREG>
+template <int PX, int PT, bool REFREG, int MINB = 1>
 cudaError_t launch_t(const Image &src, const StepParams &sp, const SearchArgs &a, size_t smem, int nsm,
                      long long n, cudaStream_t st)
 {
-	cudaError_t e = cudaFuncSetAttribute(search_kernel<PX, PT, REFREG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                                     (int)smem);
+	auto kern = search_kernel<PX, PT, REFREG, MINB>;
+	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
 	int per_sm = 0;
-	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, search_kernel<PX, PT, REFREG>, kThreads, smem);
+	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
 	if (e != cudaSuccess) return e;
 	long long blocks = (long long)nsm * (per_sm < 1 ? 1 : per_sm);
 	if (blocks > n) blocks = n;
-	search_kernel<PX, PT, REFREG><<<(int)blocks, kThreads, smem, st>>>(src, sp, a);
+	kern<<<(int)blocks, kThreads, smem, st>>>(src, sp, a);
 	return cudaGetLastError();
 }
 
@@ -661,28 +591,29 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
 	a.grid = grid;
 	a.traj = traj;
 	a.nfm = search_frames_max(sp);
-	a.BX = (sp.wx + sp.px + 2 + 3) / 4 * 4;     // window + halo + misalignment, multiple of 4
-	a.BY = sp.wx + sp.px - 1;
-	a.CB = sp.chn_search;
 	a.g_begin = g_begin;
 	a.g_end = g_end;
 	a.nsimp = nsimp;
 	a.idx = idx;
-	a.err = err;
+	(void)err;
 	const long long n = g_end - g_begin;
 	const size_t ncand = (size_t)sp.wx * sp.wx * a.nfm;
-	const size_t smem = sizeof(float) * (ncand + (size_t)sp.spc * sp.chn_search);
-	// The reference patch in shared memory (80 registers, four CTAs per SM)
-	// measured faster than in registers (168 registers, two CTAs per SM):
-	// 179 vs 231 ms on 854x480x20.  BM4DOF_SEARCH_REFREG=1 selects the
-	// register variant.
+	const size_t smem = sizeof(float) * (ncand + (((size_t)sp.spc * sp.chn_search + 3) & ~(size_t)3));
+	// The reference patch in shared memory, taken into registers one patch
+	// frame at a time, measured faster than the whole patch in registers
+	// (two CTAs per SM).  BM4DOF_SEARCH_REFREG=1 selects the register variant.
 	static const int refreg_env = [] {
 		const char *e = std::getenv("BM4DOF_SEARCH_REFREG");
 		return e ? std::atoi(e) : 0;
 	}();
 	const bool one = sp.chn_search == 1 && refreg_env != 0;
-	if (sp.px == 4 && sp.pt == 4)
-		return one ? launch_t<4, 4, true>(src, sp, a, smem, nsm, n, st) : launch_t<4, 4, false>(src, sp, a, smem, nsm, n, st);
+	if (sp.px == 4 && sp.pt == 4) {
+		// six CTAs per SM (56 registers, a few spilled) measured faster than
+		// four (80 registers) and five (64): 133 vs 137 vs 147 ms on 854x480x20
+		if (one) return launch_t<4, 4, true>(src, sp, a, smem, nsm, n, st);
+		if (sp.search_ctas == 4) return launch_t<4, 4, false, 4>(src, sp, a, smem, nsm, n, st);
+		return launch_t<4, 4, false, 6>(src, sp, a, smem, nsm, n, st);
+	}
 	if (sp.px == 8 && sp.pt == 1)
 		return one ? launch_t<8, 1, true>(src, sp, a, smem, nsm, n, st) : launch_t<8, 1, false>(src, sp, a, smem, nsm, n, st);
 	return launch_t<0, 0, false>(src, sp, a, smem, nsm, n, st);

@@ -123,6 +123,7 @@ void          bm4dof_destroy(bm4dof_ctx *ctx);
 #define BM4DOF_DEVICE_POINTERS  0x1u  /* all video pointers are device pointers  */
 #define BM4DOF_KEEP_GROUPS      0x2u  /* record neighbour lists for inspection   */
 #define BM4DOF_MIXED_PRECISION  0x4u  /* FP16 distance pre-screen + BF16 transforms */
+#define BM4DOF_LEARNED          0x8u  /* learned form: no step-1 pass (see below)  */
 
 /* VideoNLB::runNlBayes, src/core/nldct.cpp:267-478.
  *
@@ -183,6 +184,142 @@ bm4dof_status bm4dof_search_groups_noalloc(const float *video, const float *fflo
  * ms[3] everything else (copies, colour, normalisation), ms[4] the whole call
  * from its first to its last event; and the number of kernel launches. */
 bm4dof_status bm4dof_last_timings(bm4dof_ctx *ctx, float ms[5], unsigned *launches);
+
+/* ---- batched runs ----------------------------------------------------------
+ * No counterpart in the reference (its caller runs one video per process).
+ * Many sequences of uneven size, frame count and sigma denoised by one CUDA
+ * graph: each sequence's whole runNlBayes (both steps) is recorded on one of
+ * `branches` streams, the branches are joined into a single graph, and the
+ * graph is launched once.  A call with the same sequences, pointers, flags and
+ * tuning as the previous one replays the instantiated graph. */
+
+/* One sequence of a batched run.  All video pointers are device pointers. */
+typedef struct bm4dof_sequence {
+	const float *noisy, *fflow, *bflow;    /* flows: both or neither          */
+	unsigned width, height, channels, frames;
+	float *basic, *final_;
+	bm4dof_params params1, params2;
+	unsigned nparts;                       /* 0 means 2                       */
+	float ratios[2];                       /* out, as bm4dof_run              */
+} bm4dof_sequence;
+
+/* Launch shape of a batched run (bm4dof_autotune chooses one). */
+typedef struct bm4dof_tuning {
+	unsigned branches;     /* concurrent streams in the graph; 0: min(n, 16)     */
+	unsigned slot_mb;      /* per sequence: MB of aggregation terms per chunk
+	                          (the depth of group staging); 0: 1024              */
+	unsigned search_ctas;  /* exact search CTAs per SM: 4 or 6; 0: 6             */
+} bm4dof_tuning;
+
+/* Denoises n sequences (flags: BM4DOF_MIXED_PRECISION, BM4DOF_LEARNED; the
+ * pointers are always device pointers).  tuning may be NULL (defaults).
+ * bm4dof_last_timings reports the graph launch as ms[4]. */
+bm4dof_status bm4dof_run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n, unsigned flags,
+                                 const bm4dof_tuning *tuning);
+
+/* Times candidate tunings (graph replays of the first `sample` sequences,
+ * coordinate descent over branches, slot_mb and search_ctas) and returns the
+ * fastest in *best.  table (may be NULL) receives up to cap rows of
+ * {branches, slot_mb, search_ctas, milliseconds} as floats; *rows = count. */
+bm4dof_status bm4dof_autotune(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n, unsigned sample,
+                              unsigned flags, bm4dof_tuning *best, float *table, unsigned cap, unsigned *rows);
+
+/* ---- optical flow ------------------------------------------------------------
+ * TV-L1 flow (Zach, Pock and Bischof's dual method), the step the reference
+ * runs before the denoiser: lib/tvl1flow (Dual_TVL1_optic_flow_multiscale,
+ * tvl1flow_lib.c:344-474) as driven by scripts/tvl1flow-seq.sh. */
+typedef struct bm4dof_tvl1_params {
+	float tau, lambda, theta;   /* time step, data weight, coupling weight      */
+	int   nscales, fscale;      /* pyramid levels (capped as main.c:147-153 does),
+	                               finest level computed                        */
+	float zfactor;              /* pyramid factor                                */
+	int   warps;                /* warpings per level                            */
+	float epsilon;              /* stopping threshold                            */
+} bm4dof_tvl1_params;
+
+/* The values scripts/tvl1flow-seq.sh passes: 0.25 0.2 0.3 100 1 0.5 5 0.01. */
+void bm4dof_tvl1_default_params(bm4dof_tvl1_params *p);
+
+/* Flow of npairs grey frame pairs I0[k] -> I1[k] (each width x height,
+ * [pair][y][x]) into uv[k] = (u plane, v plane) ([pair][2][y][x]), as
+ * tvl1flow writes it for I0 = the first image.  Pointers follow flags
+ * (BM4DOF_DEVICE_POINTERS). */
+bm4dof_status bm4dof_tvl1_pairs(bm4dof_ctx *ctx, const float *I0, const float *I1, unsigned width,
+                                unsigned height, unsigned npairs, const bm4dof_tvl1_params *params,
+                                float *uv, unsigned flags);
+
+/* Forward and backward flows of a grey video ([frame][y][x]) in the layout
+ * bm4dof_run takes (W*H*2*F each): fflow[t] = flow t -> t+1, bflow[t] = flow
+ * t -> t-1, the last forward and the first backward field copied from their
+ * neighbours as tvl1flow-seq.sh does.  All 2(F-1) pairs are computed in one
+ * batch. */
+bm4dof_status bm4dof_tvl1_video(bm4dof_ctx *ctx, const float *video, unsigned width, unsigned height,
+                                unsigned frames, const bm4dof_tvl1_params *params, float *fflow, float *bflow,
+                                unsigned flags);
+
+/* ---- learned form ----------------------------------------------------------
+ * No counterpart in the reference.  With BM4DOF_LEARNED, bm4dof_run skips the
+ * step-1 pass: groups are searched on the noisy video with params2's geometry
+ * and filtered in the 3-D transform domain of the reference's step 2, with the
+ * Wiener gains of the member-mean Haar row predicted by the gain network
+ * (65 -> 256 -> 256 -> 64, GELU, sigmoid output, BF16 weights) from the
+ * log-variances log(mean_m Z[m][k]^2 / sigma^2) of the 64 patch coefficients
+ * across the members and sigma/255; the other Haar rows are hard-thresholded
+ * at (params1->beta * sigma)^2.  A group whose residual variance exceeds
+ * kappa * sigma^2 is filtered again by the two-step shrinkage of its own
+ * coefficients (hard-threshold pilot, then Wiener).  Grey video, 64-element
+ * patches.  `basic` receives the same estimate as `final`. */
+
+/* Floats in a gain-network parameter blob: W1[65][256] b1[256] W2[256][256]
+ * b2[256] W3[256][64] b3[64], each W[in][out]. */
+#define BM4DOF_GAIN_PARAMS 99136u
+
+/* Installs the gain network used by BM4DOF_LEARNED runs (params: host floats,
+ * n == BM4DOF_GAIN_PARAMS), or none when params is NULL: the mean-row gains
+ * are then the empirical Wiener gains of the noisy coefficients (the method
+ * without the network).  kappa: fallback threshold (0 means 1.5). */
+bm4dof_status bm4dof_set_gain_network(bm4dof_ctx *ctx, const float *params, size_t n, float kappa);
+
+/* Groups filtered and groups that fell back in the last BM4DOF_LEARNED run. */
+bm4dof_status bm4dof_learned_stats(bm4dof_ctx *ctx, unsigned long long *groups,
+                                   unsigned long long *fallbacks);
+
+/* Training pairs for the gain network.  Searches the groups of the learned
+ * form on `noisy` (grey, params2's geometry, mask switch-offs applied) and
+ * writes, for every grid group g of all tiles in processing order:
+ *   feat[g*65 + k]    network inputs,
+ *   target[g*64 + k]  the step-2 Wiener gain y^2 / (y^2 + (beta2 sigma)^2) of
+ *                     the member-mean Haar coefficient y of patch coefficient
+ *                     k of the same members in `basic` (the plain method's
+ *                     step-1 output),
+ *   valid[g]          1 for groups the filter processes, 0 otherwise.
+ * feat/target/valid are device pointers with room for cap groups; the other
+ * pointers follow `flags` (BM4DOF_DEVICE_POINTERS).  *count = number of grid
+ * groups (BM4DOF_ERR_ARGUMENT when larger than cap). */
+bm4dof_status bm4dof_gain_samples(bm4dof_ctx *ctx, const float *noisy, const float *basic,
+                                  const float *fflow, const float *bflow,
+                                  unsigned width, unsigned height, unsigned frames,
+                                  const bm4dof_params *params2, unsigned nparts, unsigned flags,
+                                  float *feat, float *target, unsigned char *valid,
+                                  size_t cap, size_t *count);
+
+/* Training of the gain network on the GPU: forward, backward (mean squared
+ * error of the 64 gains) and AdamW, BF16 operands with FP32 accumulation and
+ * FP32 master weights.  feat/target/gains are device pointers of n <= batch
+ * rows (feat [n][65], target and gains [n][64]). */
+typedef struct bm4dof_trainer bm4dof_trainer;
+bm4dof_status bm4dof_trainer_create(bm4dof_trainer **t, int device, unsigned batch, unsigned seed);
+void          bm4dof_trainer_destroy(bm4dof_trainer *t);
+/* Reads (set = 0) or writes (set = 1) the FP32 master parameters as a host blob. */
+bm4dof_status bm4dof_trainer_params(bm4dof_trainer *t, float *params, size_t n, int set);
+/* Loss and gradient (host blob, may be NULL) of one batch, no update. */
+bm4dof_status bm4dof_trainer_grad(bm4dof_trainer *t, const float *feat, const float *target, unsigned n,
+                                  float *grads, float *loss);
+/* One AdamW step (beta1 0.9, beta2 0.999, eps 1e-8; decay on the matrices). */
+bm4dof_status bm4dof_trainer_step(bm4dof_trainer *t, const float *feat, const float *target, unsigned n,
+                                  float lr, float weight_decay, float *loss);
+/* Network outputs for n rows, with the inference kernel bm4dof_run uses. */
+bm4dof_status bm4dof_trainer_predict(bm4dof_trainer *t, const float *feat, unsigned n, float *gains);
 
 #ifdef __cplusplus
 }

@@ -15,4 +15,7 @@ CASES = [
      dict(px1=8, px2=7, pt1=1, pt2=1, wx1=9, wx2=11, np1=8, np2=32), 1),
     ("rgb_image", 40, 36, 1, 3, 20.0, 19, False, CFG_IMAGE, 1),
     ("rgb_video", 30, 28, 4, 3, 20.0, 20, True, CFG_VIDEO, 1),
+    # -order-inv: one Wiener gain per coefficient for the mean row and one for the rest
+    ("video_order_inv", 40, 36, 6, 1, 20.0, 21, True, dict(CFG_VIDEO, order_inv=True), 1),
+    ("image_order_inv", 48, 40, 1, 1, 25.0, 22, False, dict(CFG_IMAGE, order_inv=True), 1),
 ]

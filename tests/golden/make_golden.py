@@ -3,7 +3,7 @@ from its sources into oracle/_ref by oracle/Makefile) on the seeded cases of
 tests/cases.py.  Inputs are stored with the outputs, so the fixtures do not
 depend on the random generator of the machine that reads them.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case names]   # default: every case
 """
 import os
 import sys
@@ -19,10 +19,12 @@ import pyoracle  # noqa: E402
 FIELDS = [f for f, _ in pyoracle.Params._fields_]
 
 
-def main():
+def main(names=()):
     pyoracle.build()
     ref = pyoracle.Reference()
     for (name, W, H, F, C, sigma, seed, flow, cli, nthreads) in CASES:
+        if names and name not in names:
+            continue
         clean, nz, ff, bf = video_case(W, H, F, sigma=sigma, seed=seed, channels=C, flow=flow)
         p1, p2 = resolve_params(ref, (W, H, F, C), sigma, **cli)
         basic, final, ratios = ref.runNlBayes(nz, ff, bf, p1, p2, nthreads=nthreads)
@@ -37,4 +39,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -29,13 +29,18 @@ def test_gpu_matches_golden(gpulib, gpuctx, case):
     p1, p2 = gparams(gpulib, g["p1"]), gparams(gpulib, g["p2"])
     nparts = 2 * int(g["nthreads"])
     basic, final, ratios = gpuctx.runNlBayes(g["noisy"], g.get("fflow"), g.get("bflow"), p1, p2, nparts=nparts)
-    db = np.abs(basic.astype(np.float64) - g["basic"]).max()
-    df = np.abs(final.astype(np.float64) - g["final"]).max()
+    # NaN where the reference makes NaN (order-invariant filtering of
+    # one-member groups divides 0 by 0, nldct.cpp:1872)
+    assert np.array_equal(np.isnan(basic), np.isnan(g["basic"]))
+    assert np.array_equal(np.isnan(final), np.isnan(g["final"]))
+    db = np.nanmax(np.abs(basic.astype(np.float64) - g["basic"]))
+    df = np.nanmax(np.abs(final.astype(np.float64) - g["final"]))
     assert db <= TOL_GREY and df <= TOL_GREY, (db, df)
-    assert abs(psnr(final, g["clean"]) - psnr(g["final"], g["clean"])) <= TOL_PSNR
+    if not np.isnan(g["final"]).any():
+        assert abs(psnr(final, g["clean"]) - psnr(g["final"], g["clean"])) <= TOL_PSNR
     # the exact path is bit-identical
-    assert np.array_equal(basic, g["basic"]), db
-    assert np.array_equal(final, g["final"]), df
+    assert np.array_equal(basic, g["basic"], equal_nan=True), db
+    assert np.array_equal(final, g["final"], equal_nan=True), df
     assert ratios == tuple(g["ratios"].tolist())
 
 

@@ -32,8 +32,10 @@ def test_oracle_matches_golden(oracle, case):
     nthreads = int(g["nthreads"])
     basic, final, ratios = oracle.runNlBayes(g["noisy"], g.get("fflow"), g.get("bflow"), p1, p2,
                                              nparts=2 * nthreads, nthreads=nthreads)
-    assert np.array_equal(basic, g["basic"])
-    assert np.array_equal(final, g["final"])
+    # NaN where the reference makes NaN (order-invariant filtering of
+    # one-member groups divides 0 by 0, nldct.cpp:1872)
+    assert np.array_equal(basic, g["basic"], equal_nan=True)
+    assert np.array_equal(final, g["final"], equal_nan=True)
     assert ratios == tuple(g["ratios"].tolist())
 
 
