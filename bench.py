@@ -412,6 +412,13 @@ def main():
             g, fb = ctx.learned_stats()
             forms[name]["fallback_groups"] = [fb, g]
     line["forms"] = forms
+    # the step before the path: TV-L1 flows of the whole video (2(F-1) frame
+    # pairs in one batch, tvl1flow-seq.sh parameters), host video in, flows out
+    ctx.tvl1_video(nz)
+    ctx.tvl1_video(nz)
+    fms = ctx.timings()[0][4]
+    line["flow"] = {"method": "TV-L1 (lib/tvl1flow), 2(F-1) pairs batched", "pairs": 2 * (F - 1), "ms": fms,
+                    "pairs_per_s": 2 * (F - 1) / (fms / 1e3)}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(nz, ff, bf, sigma)
     print(json.dumps(line), flush=True)

@@ -220,6 +220,7 @@ struct SelectShared {
 	float tmin[kThreads];
 	float bound;
 	unsigned nsel;
+	int has_nan;        // a NaN distance: only the heap replay orders it as the reference does
 	float sd[kSelCap];
 	int si[kSelCap];
 	float hd[kMaxNp];
@@ -241,7 +242,10 @@ __device__ void select_knn(const float *dist, int ncand, int K, float tmin, Sele
 {
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	S.tmin[tid] = tmin;
-	if (tid == 0) S.nsel = 0u;
+	if (tid == 0) {
+		S.nsel = 0u;
+		S.has_nan = 0;
+	}
 	__syncthreads();
 	if (warp == 0) {
 		// K-th smallest of the per-thread minima (repeated warp minimum)
@@ -272,17 +276,20 @@ __device__ void select_knn(const float *dist, int ncand, int K, float tmin, Sele
 	}
 	__syncthreads();
 	const float bound = S.bound;
+	int nan = 0;
 	for (int i = tid; i < ncand; i += blockDim.x) {
 		const float d = dist[i];
+		nan |= d != d;
 		if (d <= bound) {
 			const unsigned s = atomicAdd(&S.nsel, 1u);
 			if (s < (unsigned)kSelCap) { S.sd[s] = d; S.si[s] = i; }
 		}
 	}
+	if (__syncthreads_or(nan) && tid == 0) S.has_nan = 1;
 	__syncthreads();
 	if (warp == 0) {
 		const int n = (int)S.nsel;
-		bool ok = n >= K && n <= kSelCap;
+		bool ok = n >= K && n <= kSelCap && !S.has_nan;
 		if (ok) {
 			// bitonic sort of up to 64 (distance, candidate) pairs, 2 per lane
 			float d0 = lane < n ? S.sd[lane] : __int_as_float(0x7f800000);

@@ -52,7 +52,7 @@ def test_gpu_neighbours_match_oracle(gpulib, gpuctx, oracle, case):
     pg = resolve_params(gpulib, (W, H, F, C), sigma, **cli)
     ob, of, orat, tr = oracle.runNlBayes(nz, ff, bf, *po, nparts=2 * nthreads, trace_cap=100000, trace_stride=32)
     gb, gf, grat = gpuctx.runNlBayes(nz, ff, bf, *pg, nparts=2 * nthreads, keep_groups=True)
-    assert np.array_equal(gb, ob) and np.array_equal(gf, of)
+    assert np.array_equal(gb, ob, equal_nan=True) and np.array_equal(gf, of, equal_nan=True)
     for step in (1, 2):
         for tile in range(2 * nthreads):
             sel = (tr["step"] == step) & (tr["tile"] == tile)
