@@ -3,7 +3,8 @@
 // input, the step the reference runs before its path (lib/tvl1flow, driven by
 // scripts/tvl1flow-seq.sh).
 //
-// Restates, with the same float/double arithmetic:
+// Restates, with the same float/double arithmetic (except |grad u| of the dual
+// update, taken in float instead of the reference's double hypot):
 //   tvl1flow_lib.c   image_normalization (299-336), Dual_TVL1_optic_flow
 //                    (93-263), Dual_TVL1_optic_flow_multiscale (344-474);
 //   mask.c           divergence (40-88), forward_gradient (96-139),
@@ -307,10 +308,14 @@ __global__ void __launch_bounds__(256) iterate_kernel(IterArgs a)
 				float u1x, u1y, u2x, u2y;
 				forward_gradient_at(a.u1 + base, i, j, a.nx, a.ny, u1x, u1y);
 				forward_gradient_at(a.u2 + base, i, j, a.nx, a.ny, u2x, u2y);
-				const float g1 = (float)hypot((double)u1x, (double)u1y);
-				const float g2 = (float)hypot((double)u2x, (double)u2y);
-				const float ng1 = (float)(1.0 + (double)(taut * g1));
-				const float ng2 = (float)(1.0 + (double)(taut * g2));
+				// |grad u| in float (the reference's double hypot rounded to
+				// float agrees to the last bit or one unit; FP64 is slow here),
+				// and 1.0 + x rounded once to float, as the reference's
+				// double sum of two floats is
+				const float g1 = sqrtf(u1x * u1x + u1y * u1y);
+				const float g2 = sqrtf(u2x * u2x + u2y * u2y);
+				const float ng1 = 1.f + taut * g1;
+				const float ng2 = 1.f + taut * g2;
 				a.p11[q] = (a.p11[q] + taut * u1x) / ng1;
 				a.p12[q] = (a.p12[q] + taut * u1y) / ng1;
 				a.p21[q] = (a.p21[q] + taut * u2x) / ng2;
