@@ -18,6 +18,7 @@
 // The result is written as per-member aggregation terms (w*window[p])*g, the
 // exact float product the reference adds into its image (2296-2297, 2385-2386).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 
 #include "common.cuh"
@@ -318,6 +319,165 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
 	}
 }
 
+// ---------------------------------------------------------------------------
+// The same filter for one-channel groups of 64-element patches, four groups
+// per CTA (64 threads each, sharing the bases in shared memory).  Each thread
+// of a product forms a 4-member x 4-coefficient block, so that two vector
+// loads feed 16 multiply-add pairs; every output is still accumulated over the
+// inner index in increasing order with separately rounded products and sums,
+// so the results are the generic kernel's, bit for bit.
+// ---------------------------------------------------------------------------
+constexpr int kQuadSub = 64, kQuadGroups = 4;
+
+__device__ __forceinline__ void quad_sync(int id)
+{
+	asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(kQuadSub) : "memory");
+}
+
+// out[(q0 + c) * nsp + n0 + m] = sum_r in[r * nsp + n0 + m] * M[r * 64 + q0 + c]
+__device__ __forceinline__ void product4x4(const float *in, const float *M, float *out, int nsp, int q0, int n0)
+{
+	float a[4][4];
+#pragma unroll
+	for (int m = 0; m < 4; m++)
+#pragma unroll
+		for (int c = 0; c < 4; c++) a[m][c] = 0.f;
+#pragma unroll 4
+	for (int r = 0; r < 64; r++) {
+		const float4 g = *reinterpret_cast<const float4 *>(in + r * nsp + n0);
+		const float4 b = *reinterpret_cast<const float4 *>(M + r * 64 + q0);
+		const float gm[4] = {g.x, g.y, g.z, g.w}, bc[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+		for (int m = 0; m < 4; m++)
+#pragma unroll
+			for (int c = 0; c < 4; c++) a[m][c] = __fadd_rn(a[m][c], __fmul_rn(gm[m], bc[c]));
+	}
+#pragma unroll
+	for (int c = 0; c < 4; c++)
+		*reinterpret_cast<float4 *>(out + (q0 + c) * nsp + n0) = make_float4(a[0][c], a[1][c], a[2][c], a[3][c]);
+}
+
+template <int STEP, int PX, int PT>
+__global__ void __launch_bounds__(kQuadSub *kQuadGroups, 2)
+filter_quad_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, int ntiles, StepParams sp,
+                   const float *__restrict__ basis, const float *__restrict__ binv, const float *__restrict__ win,
+                   long long g_begin, long long g_end, const uint8_t *__restrict__ nsimp,
+                   const uint32_t *__restrict__ idx, const uint8_t *__restrict__ alive, float *__restrict__ vals,
+                   float *__restrict__ wslot, float *__restrict__ wgroup, uint8_t *__restrict__ eq)
+{
+	constexpr int SPC = PX * PX * PT;
+	static_assert(SPC == 64, "four-group filter: 64-element patches");
+	extern __shared__ __align__(16) float sm[];
+	float *Bt = sm;                 // Bt[p][k] = basis[k][p]
+	float *Bi = Bt + SPC * SPC;     // Bi[k][p] = binv[k][p]
+	float *wn = Bi + SPC * SPC;
+	const int np = sp.np, nsp = nsp_of(np), tile_f = SPC * nsp;
+	const int sub = threadIdx.x / kQuadSub, t = threadIdx.x % kQuadSub;
+	// three tiles per group: the noisy group's pixels are dead once it is
+	// transformed, so the basic group's transform and then the estimate reuse
+	// their tile
+	float *Gn = wn + SPC + sub * 3 * tile_f;   // noisy group [p][n]; basic transform; estimate
+	float *Zn = Gn + tile_f;                   // noisy transform [k][n]
+	float *Gb = Zn + tile_f;                   // basic group; later w^2 / weight shares
+	float *Zb = Gn;
+	__shared__ int s_mx[kQuadGroups][kMaxNp], s_my[kQuadGroups][kMaxNp], s_mt[kQuadGroups][kMaxNp];
+	__shared__ int s_flag[kQuadGroups][2];
+	__shared__ float s_w[kQuadGroups];
+
+	for (int i = threadIdx.x; i < SPC * SPC; i += blockDim.x) {
+		const int k = i / SPC, p = i % SPC;
+		Bt[p * SPC + k] = basis[i];
+		Bi[i] = binv[i];
+	}
+	for (int i = threadIdx.x; i < SPC; i += blockDim.x) wn[i] = win[i];
+	__syncthreads();
+
+	const float sigma2 = __fmul_rn(sp.sigma, sp.sigma);
+	const float bsig = __fmul_rn(sp.beta, sp.sigma);
+	const float bs2 = __fmul_rn(bsig, bsig);
+	const float bmsig = __fmul_rn(sp.beta_mean, sp.sigma);
+	const float bm2 = __fmul_rn(bmsig, bmsig);
+	const bool oinv = sp.order_inv != 0;
+	const float is2 = (float)(1.0 / sqrt(2.0));
+	const int bar = 1 + sub, lane = t & 31, w = t >> 5;
+	const int ht = t / (PX * PX), hy = (t / PX) % PX, hx = t % PX;
+
+	for (long long g = g_begin + (long long)blockIdx.x * kQuadGroups + sub; g < g_end;
+	     g += (long long)gridDim.x * kQuadGroups) {
+		if (!alive[g]) continue;
+		const int ns = nsimp[g];
+		const Tile T = tiles[tile_of(tiles, ntiles, g)];
+		if (t < ns) {
+			const uint32_t lin = idx[g * np + t];
+			const uint32_t whl = (uint32_t)T.w * T.h;
+			s_mt[sub][t] = (int)(lin / whl);
+			s_my[sub][t] = (int)((lin % whl) / T.w);
+			s_mx[sub][t] = (int)(lin % T.w);
+		}
+		quad_sync(bar);
+		// gather the group, thread t holding patch element t of every member
+		for (int n = 0; n < ns; n++) {
+			const size_t a = noisy.at(T.ox + s_mx[sub][n] + hx, T.oy + s_my[sub][n] + hy, s_mt[sub][n] + ht, 0);
+			Gn[t * nsp + n] = __ldg(noisy.p + a);
+			if (STEP == 2) Gb[t * nsp + n] = __ldg(basic.p + a);
+		}
+		quad_sync(bar);
+		const long long slot0 = (g - g_begin) * np;
+		// all-equal test (nldct.cpp:1986-1999, 2222-2235), row t
+		int differs = 0;
+		for (int n = 1; n < ns; n++) differs |= Gn[t * nsp + n] != Gn[t * nsp];
+		differs = __any_sync(0xffffffffu, differs);
+		if (lane == 0) s_flag[sub][w] = differs;
+		quad_sync(bar);
+		if (ns > 1 && !(s_flag[sub][0] | s_flag[sub][1])) {
+			for (int n = 0; n < ns; n++) vals[(slot0 + n) * SPC + t] = Gn[t * nsp + n];
+			if (t == 0) eq[g] = 1;
+			quad_sync(bar);
+			continue;
+		}
+		// forward transform(s) in 4 x 4 blocks: noisy, then basic (over the
+		// noisy pixels)
+		const int nblk = (ns + 3) / 4;
+		for (int it = t; it < nblk * 16; it += kQuadSub) product4x4(Gn, Bt, Zn, nsp, (it % 16) * 4, (it / 16) * 4);
+		quad_sync(bar);
+		if (STEP == 2) {
+			for (int it = t; it < nblk * 16; it += kQuadSub) product4x4(Gb, Bt, Zb, nsp, (it % 16) * 4, (it / 16) * 4);
+			quad_sync(bar);
+		}
+		// Haar, shrinkage, inverse Haar of coefficient t
+		int kept = shrink_dispatch<STEP>(ns, Zn + t * nsp, Zb + t * nsp, Gb + t * ns, t, bs2, is2, oinv, sigma2, bm2,
+		                                 Gb + t);
+		if (STEP == 1 && !oinv) {
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+			if (lane == 0) s_flag[sub][w] = kept;
+		}
+		quad_sync(bar);
+		if (t == 0) {
+			if (oinv) {
+				float v = 0.f;   // float sum of the coefficients' shares in k order
+				for (int i = 0; i < SPC; i++) v = __fadd_rn(v, Gb[i]);
+				s_w[sub] = STEP == 1 ? __fdiv_rn(__fdiv_rn(1.f, sigma2), v) : (float)(1.0 / (double)sigma2 / (double)v);
+			} else if (STEP == 1) {
+				s_w[sub] = __fdiv_rn(__fdiv_rn(1.f, sigma2), (float)(s_flag[sub][0] + s_flag[sub][1]));
+			} else {
+				float v = 0.f;   // sum of w^2 in the reference's (k, n) order
+				for (int i = 0; i < SPC * ns; i++) v = __fadd_rn(v, Gb[i]);
+				s_w[sub] = (float)(1.0 / (double)sigma2 / (double)v);
+			}
+		}
+		// inverse transform into Gn
+		for (int it = t; it < nblk * 16; it += kQuadSub) product4x4(Zn, Bi, Gn, nsp, (it % 16) * 4, (it / 16) * 4);
+		quad_sync(bar);
+		const float wg = s_w[sub];
+		const float wp = __fmul_rn(wg, wn[t]);
+		for (int n = 0; n < ns; n++) vals[(slot0 + n) * SPC + t] = __fmul_rn(wp, Gn[t * nsp + n]);
+		if (t < ns) wslot[slot0 + t] = wg;
+		if (t == 0) { wgroup[g] = wg; eq[g] = 0; }
+		quad_sync(bar);
+	}
+}
+
 // Groups whose members are all equal keep the aggregation weights left by the
 // previous processed groups of their tile (the reference's aggreWeights vector
 // is not rewritten, nldct.cpp:1998, 2234): member n takes the weight of the
@@ -374,6 +534,24 @@ cudaError_t launch_exact(int blocks, size_t smem, cudaStream_t st, const Image &
 	return cudaGetLastError();
 }
 
+template <int STEP, int PX, int PT>
+cudaError_t launch_quad(int blocks, size_t smem, cudaStream_t st, const Image &noisy, const Image &basic,
+                        const Tile *tiles, int ntiles, const StepParams &sp, const float *basis, const float *binv,
+                        const float *win, long long g_begin, long long g_end, const uint8_t *nsimp,
+                        const uint32_t *idx, const uint8_t *alive, float *vals, float *wslot, float *wgroup,
+                        uint8_t *eq)
+{
+	auto kern = filter_quad_kernel<STEP, PX, PT>;
+	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess) return e;
+	kern<<<blocks, kQuadSub * kQuadGroups, smem, st>>>(noisy, basic, tiles, ntiles, sp, basis, binv, win, g_begin,
+	                                                  g_end, nsimp, idx, alive, vals, wslot, wgroup, eq);
+	return cudaGetLastError();
+}
+
+#define FILTER_ARGS_NB noisy, basic, tiles, ntiles, sp, basis, binv, win, g_begin, g_end, nsimp, idx, alive, vals, \
+	    wslot, wgroup, eq
+
 #define FILTER_ARGS                                                                                   \
 	blocks, smem, st, noisy, basic, tiles, ntiles, sp, basis, binv, win, g_begin, g_end, nsimp, idx, alive, \
 	    vals, wslot, wgroup, eq
@@ -392,7 +570,15 @@ cudaError_t launch_filter(const Image &noisy, const Image &basic, const Tile *ti
 	const long long n = g_end - g_begin;
 	const int blocks = (int)(n < (long long)nsm * 8 ? n : (long long)nsm * 8);
 	cudaError_t e;
-	if (sp.C == 1 && sp.px == 4 && sp.pt == 4)
+	if (sp.C == 1 && sp.spc == 64 && ((sp.px == 4 && sp.pt == 4) || (sp.px == 8 && sp.pt == 1))) {
+		const size_t qsmem = sizeof(float) * (2 * 64 * 64 + 64 + (size_t)kQuadGroups * 3 * 64 * (((sp.np + 3) / 4) * 4 + 4));
+		const long long need = (n + kQuadGroups - 1) / kQuadGroups;
+		const int qb = (int)std::min<long long>(need, (long long)nsm * 2);
+		if (sp.px == 4)
+			e = sp.step1 ? launch_quad<1, 4, 4>(qb, qsmem, st, FILTER_ARGS_NB) : launch_quad<2, 4, 4>(qb, qsmem, st, FILTER_ARGS_NB);
+		else
+			e = sp.step1 ? launch_quad<1, 8, 1>(qb, qsmem, st, FILTER_ARGS_NB) : launch_quad<2, 8, 1>(qb, qsmem, st, FILTER_ARGS_NB);
+	} else if (sp.C == 1 && sp.px == 4 && sp.pt == 4)
 		e = sp.step1 ? launch_exact<1, 4, 4, 1>(FILTER_ARGS) : launch_exact<2, 4, 4, 1>(FILTER_ARGS);
 	else if (sp.C == 1 && sp.px == 8 && sp.pt == 1)
 		e = sp.step1 ? launch_exact<1, 8, 1, 1>(FILTER_ARGS) : launch_exact<2, 8, 1, 1>(FILTER_ARGS);

@@ -293,6 +293,251 @@ learned_kernel(LearnedArgs a, StepParams sp)
 	}
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core form of the features and apply kernels (groups of at most 16
+// members): one warp per group; the patch transform and its inverse are
+// m16n8k16 BF16 products with FP32 accumulation (members x 64 coefficients, K =
+// 64), the Haar transform and the shrinkage stay in FP32 on the coefficients,
+// one or two columns per lane.
+// ---------------------------------------------------------------------------
+constexpr int kTcWarps = 8;
+constexpr int kBP = 72;    // bf16 row pitch of the 64-wide tiles
+constexpr int kZP = 17;    // fp32 pitch of the [coefficient][member] tile
+
+struct TcWarp {
+	__nv_bfloat16 A[16][kBP];   // members x pixels, then members x shrunk coefficients
+	float G[16][64];            // the group's pixels (FP32)
+	float Z[64][kZP];           // coefficients x members, then pixels x members (estimate)
+};
+
+__device__ __forceinline__ void mma_bf16_tc(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                            uint32_t b0, uint32_t b1)
+{
+	asm volatile(
+	    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+	    "{%0,%1,%2,%3};\n"
+	    : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+	    : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// OUT[row m][col n] = sum_k A[m][k] * Bt[n][k]; result rows scattered into
+// Z[n][m] (m < 16, n < 64)
+__device__ __forceinline__ void tc_product(const __nv_bfloat16 (*A)[kBP], const __nv_bfloat16 *Bt, float (*Z)[kZP])
+{
+	const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	float acc[8][4];
+#pragma unroll
+	for (int j = 0; j < 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+	for (int k0 = 0; k0 < 64; k0 += 16) {
+		const uint32_t a0 = *reinterpret_cast<const uint32_t *>(&A[g][k0 + 2 * t]);
+		const uint32_t a1 = *reinterpret_cast<const uint32_t *>(&A[g + 8][k0 + 2 * t]);
+		const uint32_t a2 = *reinterpret_cast<const uint32_t *>(&A[g][k0 + 8 + 2 * t]);
+		const uint32_t a3 = *reinterpret_cast<const uint32_t *>(&A[g + 8][k0 + 8 + 2 * t]);
+#pragma unroll
+		for (int j = 0; j < 8; j++) {
+			const __nv_bfloat16 *b = Bt + (j * 8 + g) * kBP + k0 + 2 * t;
+			mma_bf16_tc(acc[j], a0, a1, a2, a3, *reinterpret_cast<const uint32_t *>(b),
+			            *reinterpret_cast<const uint32_t *>(b + 8));
+		}
+	}
+#pragma unroll
+	for (int j = 0; j < 8; j++) {
+		const int n = j * 8 + 2 * t;
+		Z[n][g] = acc[j][0];
+		Z[n + 1][g] = acc[j][1];
+		Z[n][g + 8] = acc[j][2];
+		Z[n + 1][g + 8] = acc[j][3];
+	}
+}
+
+template <int NS>
+__device__ __forceinline__ void tc_column(const LearnedArgs &a, const StepParams &sp, long long r, int k,
+                                          TcWarp &W, float &w2, float (&zh)[NS], bool fallback)
+{
+	const float bs2 = (sp.beta * sp.sigma) * (sp.beta * sp.sigma);
+	const float bt2 = (sp.beta1 * sp.sigma) * (sp.beta1 * sp.sigma);
+	float z[NS];
+	if (!fallback) {
+#pragma unroll
+		for (int m = 0; m < NS; m++) zh[m] = W.Z[k][m];
+		haar_fwd<NS>(zh);
+		float gain;
+		if (a.gains) {
+			gain = a.gains[r * kSpc + k];
+		} else {
+			const float dd = zh[0] * zh[0];
+			gain = dd > bs2 ? (dd - bs2) / dd : 0.f;
+		}
+		w2 = gain * gain;
+		z[0] = zh[0] * gain;
+#pragma unroll
+		for (int m = 1; m < NS; m++) {
+			const float pilot = zh[m] * zh[m] > bt2 ? zh[m] : 0.f;
+			const float pp = pilot * pilot;
+			const float w = pp / (pp + bs2);
+			z[m] = zh[m] * w;
+			w2 = fmaf(w, w, w2);
+		}
+	} else {
+		w2 = 0.f;
+#pragma unroll
+		for (int m = 0; m < NS; m++) {
+			const float pilot = (zh[m] * zh[m] > bt2 || (k == 0 && m == 0)) ? zh[m] : 0.f;
+			const float pp = pilot * pilot;
+			const float w = pp / (pp + bs2);
+			z[m] = zh[m] * w;
+			w2 = fmaf(w, w, w2);
+		}
+	}
+	haar_inv<NS>(z);
+#pragma unroll
+	for (int m = 0; m < NS; m++) W.A[m][k] = __float2bfloat16_rn(z[m]);
+}
+
+template <int NS, int MODE>
+__device__ void tc_group(const LearnedArgs &a, const StepParams &sp, long long g, TcWarp &W,
+                         const __nv_bfloat16 *Bs, const __nv_bfloat16 *Bit, const float *win)
+{
+	const int lane = threadIdx.x & 31;
+	const float sigma2 = sp.sigma * sp.sigma;
+	const long long r = g - a.ga;
+	tc_product(W.A, Bs, W.Z);
+	__syncwarp();
+	if (MODE == kLearnedFeatures) {
+		__nv_bfloat16 *row = a.feat + r * kMlpInPad;
+#pragma unroll
+		for (int h = 0; h < 2; h++) {
+			const int k = lane + 32 * h;
+			float var = 0.f;
+#pragma unroll
+			for (int m = 0; m < NS; m++) var = fmaf(W.Z[k][m], W.Z[k][m], var);
+			row[k] = __float2bfloat16_rn(feature_of(var / (float)NS, sigma2));
+		}
+		if (lane == 0) row[kSpc] = __float2bfloat16_rn(sp.sigma / 255.f);
+		if (lane < kMlpInPad - kSpc - 1) row[kSpc + 1 + lane] = __float2bfloat16_rn(0.f);
+		return;
+	}
+	float zh0[NS], zh1[NS], w2a, w2b;
+	tc_column<NS>(a, sp, r, lane, W, w2a, zh0, false);
+	tc_column<NS>(a, sp, r, lane + 32, W, w2b, zh1, false);
+	__syncwarp();
+	tc_product(W.A, Bit, W.Z);   // estimate, [pixel][member]
+	__syncwarp();
+	float res = 0.f;
+#pragma unroll
+	for (int h = 0; h < 2; h++) {
+		const int p = lane + 32 * h;
+#pragma unroll
+		for (int m = 0; m < NS; m++) {
+			const float d = W.G[m][p] - W.Z[p][m];
+			res = fmaf(d, d, res);
+		}
+	}
+	float w2 = w2a + w2b;
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		res += __shfl_xor_sync(0xffffffffu, res, o);
+		w2 += __shfl_xor_sync(0xffffffffu, w2, o);
+	}
+	if (res > a.kappa * sigma2 * (float)(NS * kSpc)) {
+		// fallback: two-step shrinkage of the group's own coefficients
+		__syncwarp();
+		tc_column<NS>(a, sp, r, lane, W, w2a, zh0, true);
+		tc_column<NS>(a, sp, r, lane + 32, W, w2b, zh1, true);
+		__syncwarp();
+		tc_product(W.A, Bit, W.Z);
+		__syncwarp();
+		w2 = w2a + w2b;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) w2 += __shfl_xor_sync(0xffffffffu, w2, o);
+		if (lane == 0) atomicAdd(a.nfallback, 1u);
+	}
+	const float wgt = 1.f / (sigma2 * fmaxf(w2, 1e-3f));
+	const long long slot0 = r * sp.np;
+#pragma unroll
+	for (int h = 0; h < 2; h++) {
+		const int p = lane + 32 * h;
+		const float wp = wgt * win[p];
+#pragma unroll
+		for (int m = 0; m < NS; m++) a.vals[(slot0 + m) * kSpc + p] = wp * W.Z[p][m];
+	}
+	if (lane < NS) a.wslot[slot0 + lane] = wgt;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(32 * kTcWarps, 2)
+learned_tc_kernel(LearnedArgs a, StepParams sp)
+{
+	extern __shared__ __align__(16) unsigned char tsm[];
+	__nv_bfloat16 *Bs = reinterpret_cast<__nv_bfloat16 *>(tsm);    // [k][p] = basis[k][p]
+	__nv_bfloat16 *Bit = Bs + 64 * kBP;                             // [p][k] = binv[k][p]
+	float *win = reinterpret_cast<float *>(Bit + 64 * kBP);
+	TcWarp *Ws = reinterpret_cast<TcWarp *>(win + 64);
+	__shared__ int s_m[kTcWarps][3][16];
+	for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
+		const int k = i / 64, p = i % 64;
+		Bs[k * kBP + p] = __float2bfloat16_rn(a.basis[i]);
+		Bit[p * kBP + k] = __float2bfloat16_rn(a.binv[i]);
+	}
+	for (int i = threadIdx.x; i < 64; i += blockDim.x) win[i] = a.win[i];
+	__syncthreads();
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	TcWarp &W = Ws[warp];
+	const int px = sp.px;
+	for (long long g = a.ga + (long long)blockIdx.x * kTcWarps + warp; g < a.gb;
+	     g += (long long)gridDim.x * kTcWarps) {
+		if (!a.alive[g]) continue;
+		const int ns = a.nsimp[g];
+		const Tile T = a.tiles[tile_of(a.tiles, a.ntiles, g)];
+		if (lane < ns) {
+			const uint32_t lin = a.idx[g * sp.np + lane];
+			const uint32_t whl = (uint32_t)T.w * T.h;
+			s_m[warp][2][lane] = (int)(lin / whl);
+			s_m[warp][1][lane] = (int)((lin % whl) / T.w);
+			s_m[warp][0][lane] = (int)(lin % T.w);
+		}
+		__syncwarp();
+		for (int m = 0; m < 16; m++)
+#pragma unroll
+			for (int h = 0; h < 2; h++) {
+				const int p = lane + 32 * h;
+				float v = 0.f;
+				if (m < ns) {
+					const int ht = p / (px * px), hy = (p / px) % px, hx = p % px;
+					v = __ldg(a.noisy.p + a.noisy.at(T.ox + s_m[warp][0][m] + hx, T.oy + s_m[warp][1][m] + hy,
+					                                   s_m[warp][2][m] + ht, 0));
+				}
+				W.G[m][p] = v;
+				W.A[m][p] = __float2bfloat16_rn(v);
+			}
+		__syncwarp();
+		switch (ns) {
+		case 1: tc_group<1, MODE>(a, sp, g, W, Bs, Bit, win); break;
+		case 2: tc_group<2, MODE>(a, sp, g, W, Bs, Bit, win); break;
+		case 4: tc_group<4, MODE>(a, sp, g, W, Bs, Bit, win); break;
+		case 8: tc_group<8, MODE>(a, sp, g, W, Bs, Bit, win); break;
+		default: tc_group<16, MODE>(a, sp, g, W, Bs, Bit, win); break;
+		}
+		__syncwarp();
+	}
+}
+
+template <int MODE>
+cudaError_t launch_tc(const LearnedArgs &a, const StepParams &sp, int nsm, cudaStream_t st)
+{
+	const size_t smem = sizeof(__nv_bfloat16) * 2 * 64 * kBP + sizeof(float) * 64 + sizeof(TcWarp) * kTcWarps;
+	cudaError_t e = cudaFuncSetAttribute(learned_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess) return e;
+	int per_sm = 0;
+	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, learned_tc_kernel<MODE>, 32 * kTcWarps, smem);
+	if (e != cudaSuccess) return e;
+	const long long need = (a.gb - a.ga + kTcWarps - 1) / kTcWarps;
+	const long long nb = std::min<long long>(need, (long long)nsm * std::max(per_sm, 1) * 4);
+	learned_tc_kernel<MODE><<<(int)std::max<long long>(nb, 1), 32 * kTcWarps, smem, st>>>(a, sp);
+	return cudaGetLastError();
+}
+
 template <int MODE>
 cudaError_t launch_mode(const LearnedArgs &a, const StepParams &sp, int nsm, cudaStream_t st)
 {
@@ -320,9 +565,11 @@ bool learned_supported(const StepParams &sp)
 cudaError_t launch_learned(int mode, const LearnedArgs &a, const StepParams &sp, int nsm, cudaStream_t st)
 {
 	if (a.gb <= a.ga) return cudaSuccess;
+	// groups of up to 16 members: BF16 tensor-core transforms
+	const bool tc = sp.np <= 16;
 	switch (mode) {
-	case kLearnedFeatures: return launch_mode<kLearnedFeatures>(a, sp, nsm, st);
-	case kLearnedApply: return launch_mode<kLearnedApply>(a, sp, nsm, st);
+	case kLearnedFeatures: return tc ? launch_tc<kLearnedFeatures>(a, sp, nsm, st) : launch_mode<kLearnedFeatures>(a, sp, nsm, st);
+	case kLearnedApply: return tc ? launch_tc<kLearnedApply>(a, sp, nsm, st) : launch_mode<kLearnedApply>(a, sp, nsm, st);
 	default: return launch_mode<kLearnedSamples>(a, sp, nsm, st);
 	}
 }
