@@ -15,6 +15,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libbm4dof_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libbm4dof_ref.so")
+# the reference built with its VBM3D_SEARCH switch (predictive patch search)
+REF_VBM3D_SO = os.path.join(HERE, "_ref", "libbm4dof_ref_vbm3d.so")
 REF_ROOT_DEFAULT = "/root/reference"
 
 

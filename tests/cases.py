@@ -19,3 +19,13 @@ CASES = [
     ("video_order_inv", 40, 36, 6, 1, 20.0, 21, True, dict(CFG_VIDEO, order_inv=True), 1),
     ("image_order_inv", 48, 40, 1, 1, 25.0, 22, False, dict(CFG_IMAGE, order_inv=True), 1),
 ]
+
+# The reference built with its VBM3D_SEARCH switch: predictive search (the
+# best nSimilarPatchesPred matches of each frame seed small windows in the
+# next), parameters from that build's initializeNlbParameters.
+VBM3D_CASES = [
+    ("vbm3d_video", 40, 36, 6, 1, 20.0, 31, True, CFG_VIDEO, 1),
+    ("vbm3d_video_4tiles", 44, 40, 6, 1, 30.0, 32, True, CFG_VIDEO, 2),
+    ("vbm3d_noflow", 36, 32, 5, 1, 20.0, 33, False, CFG_VIDEO, 1),
+    ("vbm3d_rgb", 30, 28, 4, 3, 20.0, 34, True, CFG_VIDEO, 1),
+]

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 from helpers import resolve_params, video_case  # noqa: E402
-from cases import CASES  # noqa: E402
+from cases import CASES, VBM3D_CASES  # noqa: E402
 import pyoracle  # noqa: E402
 
 FIELDS = [f for f, _ in pyoracle.Params._fields_]
@@ -21,10 +21,17 @@ FIELDS = [f for f, _ in pyoracle.Params._fields_]
 
 def main(names=()):
     pyoracle.build()
-    ref = pyoracle.Reference()
-    for (name, W, H, F, C, sigma, seed, flow, cli, nthreads) in CASES:
-        if names and name not in names:
-            continue
+    refs = {False: pyoracle.Reference(), True: pyoracle.Reference(pyoracle.REF_VBM3D_SO)}
+    for vbm3d, cases in ((False, CASES), (True, VBM3D_CASES)):
+        for case in cases:
+            if names and case[0] not in names:
+                continue
+            make_case(refs[vbm3d], case)
+
+
+def make_case(ref, case):
+    (name, W, H, F, C, sigma, seed, flow, cli, nthreads) = case
+    if True:
         clean, nz, ff, bf = video_case(W, H, F, sigma=sigma, seed=seed, channels=C, flow=flow)
         p1, p2 = resolve_params(ref, (W, H, F, C), sigma, **cli)
         basic, final, ratios = ref.runNlBayes(nz, ff, bf, p1, p2, nthreads=nthreads)
