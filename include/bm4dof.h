@@ -124,6 +124,17 @@ void          bm4dof_destroy(bm4dof_ctx *ctx);
 #define BM4DOF_KEEP_GROUPS      0x2u  /* record neighbour lists for inspection   */
 #define BM4DOF_MIXED_PRECISION  0x4u  /* FP16 distance pre-screen + BF16 transforms */
 #define BM4DOF_LEARNED          0x8u  /* learned form: no step-1 pass (see below)  */
+/* The predictive patch search of the reference built with -DVBM3D_SEARCH
+ * (src/core/nldct.cpp:892-1130, 1351-1589) instead of the exhaustive one:
+ * the full sizeSearchWindow window in the reference frame only; in every other
+ * frame nSimilarPatchesPred windows of sizeSearchWindowPred, one around each
+ * of the previous frame's nSimilarPatchesPred best matches moved along the
+ * flow; distances on channel 0 (in step 2 summed once per channel, as the
+ * reference does), minus dsub^2*255 at the reference position of every frame;
+ * the best nSimilarPatchesPred of each frame pooled, the best nSimilarPatches
+ * of the pool kept.  Exact: the same neighbours as that build.  Plain FP32
+ * path only (not with BM4DOF_MIXED_PRECISION or BM4DOF_LEARNED). */
+#define BM4DOF_VBM3D_SEARCH     0x10u
 
 /* VideoNLB::runNlBayes, src/core/nldct.cpp:267-478.
  *

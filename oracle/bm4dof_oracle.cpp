@@ -581,6 +581,141 @@ unsigned search(const Vid &im, const Vid *basic, const Vid &fflow, const Vid &bf
 }
 
 /* ------------------------------------------------------------------------ */
+/* Predictive patch search, the reference built with VBM3D_SEARCH            */
+/* (nldct.cpp:892-1130 step 1, 1351-1589 step 2).                            */
+/* ------------------------------------------------------------------------ */
+unsigned search_vbm3d(const Vid &im, const Vid *basic, const Vid &fflow, const Vid &bflow,
+                      unsigned pidx, const bm4dof_params &p, std::vector<unsigned> &index,
+                      std::vector<std::pair<float, unsigned> > &distance)
+{
+	const bool step1 = basic == nullptr;
+	const int sPx = p.sizePatch, sPt = p.sizePatchTime;
+	unsigned nSimP = 1;
+	if (p.nSimilarPatches <= 1) { index[0] = pidx; return 1; }
+
+	/* distances on channel 0 only: the noisy video in step 1; in step 2 the
+	 * basic estimate, channel 0 summed once per channel (the loop over c of
+	 * nldct.cpp:1501-1506 never indexes the channel) */
+	const Vid &src = step1 ? im : *basic;
+	const int reps = step1 ? 1 : (int)im.c;
+	const unsigned npf = p.nSimilarPatchesPred;
+	const float dsub = p.dsub * p.dsub * 255;
+	const float tau = p.tau * p.tau * sPx * sPx * sPt;
+	const bool use_flow = fflow.w > 0;
+	const int W = im.w, H = im.h, F = im.f;
+	const int wtf = p.sizeSearchTimeRangeFwd, wtb = p.sizeSearchTimeRangeBwd;
+
+	const int pt = (int)(pidx / im.whc());
+	const int py = (int)((pidx % im.wh()) / im.w);
+	const int px = (int)(pidx % im.w);
+
+	/* temporal range and visiting order as in the exhaustive search: 934-956 */
+	const int shift_t = std::min(0, pt - wtb) + std::max(0, pt + wtf - F + sPt);
+	const int t0 = std::max(0, pt - wtb - shift_t);
+	const int t1 = std::min(F - sPt, pt + wtf - shift_t);
+	const int sWt = t1 - t0 + 1;
+	std::vector<int> order;
+	order.push_back(pt);
+	for (int qt = pt + 1; qt <= t1; ++qt) order.push_back(qt);
+	for (int qt = pt - 1; qt >= t0; --qt) order.push_back(qt);
+
+	const unsigned sPC = sPx * sPx * sPt;
+	std::vector<float> ref(sPC);
+	for (int ht = 0, k = 0; ht < sPt; ht++)
+		for (int hy = 0; hy < sPx; hy++)
+			for (int hx = 0; hx < sPx; hx++, k++)
+				ref[k] = src.at(px + hx, py + hy, pt + ht, 0);
+
+	/* trajectories: the npf best matches of each frame (961-963) */
+	std::vector<int> trx((size_t)npf * sWt, 0), try_((size_t)npf * sWt, 0), trt((size_t)npf * sWt, 0);
+	distance.clear();
+	std::vector<std::pair<float, unsigned> > dframe;
+	struct Box { int x0, y0, x1, y1; };
+	std::vector<Box> boxes;
+	for (int ii = 0; ii < sWt; ++ii) {
+		const int qt = order[ii];
+		const int dt = qt - t0;
+		const int dir = std::max(-1, std::min(1, qt - pt));
+		std::vector<int> cx, cy;
+		int sW;
+		if (dir != 0) {
+			/* one small window around each match of the previous frame, moved
+			 * along the flow, rounded half away from zero and clamped: 978-993 */
+			sW = (int)p.sizeSearchWindowPred;
+			for (unsigned i = 0; i < npf; i++) {
+				const size_t o = (size_t)i * sWt + (dt - dir);
+				const int x0 = trx[o], y0 = try_[o], f0 = trt[o];
+				const Vid &fl = dir > 0 ? fflow : bflow;
+				const float xf = x0 + (use_flow ? fl.at(x0, y0, f0, 0) : 0.f);
+				const float yf = y0 + (use_flow ? fl.at(x0, y0, f0, 1) : 0.f);
+				cx.push_back((int)std::max(0.f, std::min(W - 1.f, roundf(xf))));
+				cy.push_back((int)std::max(0.f, std::min(H - 1.f, roundf(yf))));
+			}
+		} else {
+			/* one full window around the reference patch: 995-1001 */
+			sW = (int)p.sizeSearchWindow;
+			cx.push_back(px);
+			cy.push_back(py);
+		}
+		/* windows shifted into the frame (1017-1027); their union in window,
+		 * then raster order, each position once (1033-1035) */
+		boxes.clear();
+		dframe.clear();
+		for (size_t i = 0; i < cx.size(); i++) {
+			int shx = std::min(0, cx[i] - (sW - 1) / 2);
+			int shy = std::min(0, cy[i] - (sW - 1) / 2);
+			shx += std::max(0, cx[i] + (sW - 1) / 2 - W + sPx);
+			shy += std::max(0, cy[i] + (sW - 1) / 2 - H + sPx);
+			Box b;
+			b.x0 = std::max(0, cx[i] - (sW - 1) / 2 - shx);
+			b.y0 = std::max(0, cy[i] - (sW - 1) / 2 - shy);
+			b.x1 = std::min(W - sPx, cx[i] + (sW - 1) / 2 - shx);
+			b.y1 = std::min(H - sPx, cy[i] + (sW - 1) / 2 - shy);
+			for (int qy = b.y0; qy <= b.y1; qy++)
+				for (int qx = b.x0; qx <= b.x1; qx++) {
+					bool seen = false;
+					for (const Box &o : boxes)
+						seen = seen || (qx >= o.x0 && qx <= o.x1 && qy >= o.y0 && qy <= o.y1);
+					if (seen) continue;
+					float dist = 0.f;
+					for (int r = 0; r < reps; r++)
+						for (int ht = 0, k = 0; ht < sPt; ht++)
+							for (int hy = 0; hy < sPx; hy++)
+								for (int hx = 0; hx < sPx; hx++, k++) {
+									const float dif = ref[k] - src.at(qx + hx, qy + hy, qt + ht, 0);
+									dist = dist + dif * dif;
+								}
+					/* bias towards the reference position, in every frame: 1047 */
+					if (qy == py && qx == px) dist = dist - dsub;
+					dframe.push_back(std::make_pair(dist, (unsigned)(qt * im.whc() + qy * im.w + qx)));
+				}
+			boxes.push_back(b);
+		}
+		/* the npf best of this frame feed the trajectories and the pool: 1055-1072 */
+		std::partial_sort(dframe.begin(), dframe.begin() + npf, dframe.end(), less_first);
+		for (unsigned i = 0; i < npf; i++) {
+			distance.push_back(dframe[i]);
+			const unsigned id = dframe[i].second;
+			const size_t o = (size_t)i * sWt + dt;
+			trt[o] = (int)(id / im.whc());
+			try_[o] = (int)((id % im.wh()) / im.w);
+			trx[o] = (int)(id % im.w);
+		}
+	}
+
+	/* the np best of the pool, then the power-of-two truncation by tau: 1075-1104 */
+	nSimP = std::min(p.nSimilarPatches, (unsigned)distance.size());
+	std::partial_sort(distance.begin(), distance.begin() + nSimP, distance.end(), less_first);
+	{
+		unsigned n = 1;
+		while (2 * n <= nSimP && distance[n].first < tau) n *= 2;
+		nSimP = n;
+	}
+	for (unsigned n = 0; n < nSimP; n++) index[n] = distance[n].second;
+	return nSimP;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Group filters (nldct.cpp:1799-2006 step 1, 2015-2242 step 2).             */
 /* ------------------------------------------------------------------------ */
 struct Work {
@@ -714,7 +849,7 @@ bool filter_step2(std::vector<float> &gN, std::vector<float> &gB, Work &w,
 /* ------------------------------------------------------------------------ */
 unsigned process_tile(const Vid &noisy, const Vid &fflow, const Vid &bflow, Vid &basic,
                       Vid &out, const bm4dof_params &p, const Crop &crop,
-                      std::vector<GroupTrace> *trace)
+                      std::vector<GroupTrace> *trace, bool vbm3d)
 {
 	const bool step1 = p.isFirstStep;
 	const unsigned sWx = p.sizeSearchWindow;
@@ -769,8 +904,9 @@ unsigned process_tile(const Vid &noisy, const Vid &fflow, const Vid &bflow, Vid 
 				if (!mask[(size_t)t * wh + y * W + x]) continue;
 				groups++;
 				const unsigned ij3 = t * whc + y * W + x;
-				const unsigned nS = search(noisy, step1 ? nullptr : &basic, fflow, bflow,
-				                           ij3, p, index, distance);
+				const unsigned nS = vbm3d
+					? search_vbm3d(noisy, step1 ? nullptr : &basic, fflow, bflow, ij3, p, index, distance)
+					: search(noisy, step1 ? nullptr : &basic, fflow, bflow, ij3, p, index, distance);
 				if (trace) {
 					GroupTrace g;
 					g.ref = ij3; g.nsimp = nS;
@@ -916,12 +1052,16 @@ void oracle_color_transform(float *v, unsigned W, unsigned H, unsigned C, unsign
 	std::copy(x.d.begin(), x.d.end(), v);
 }
 
-/* VideoNLB::runNlBayes, nldct.cpp:267-478, with an explicit tile count. */
-int oracle_run(const float *noisy_in, const float *fflow_in, const float *bflow_in,
-               unsigned W, unsigned H, unsigned C, unsigned F, float *basic_io, float *final_out,
-               const bm4dof_params *p1, const bm4dof_params *p2, unsigned nparts,
-               unsigned nthreads, float ratios[2], oracle_trace *trace, char *err, size_t errlen)
+/* VideoNLB::runNlBayes, nldct.cpp:267-478, with an explicit tile count;
+ * flags & BM4DOF_VBM3D_SEARCH selects the predictive search of the
+ * reference's VBM3D_SEARCH build. */
+int oracle_run_ex(const float *noisy_in, const float *fflow_in, const float *bflow_in,
+                  unsigned W, unsigned H, unsigned C, unsigned F, float *basic_io, float *final_out,
+                  const bm4dof_params *p1, const bm4dof_params *p2, unsigned nparts,
+                  unsigned nthreads, unsigned flags, float ratios[2], oracle_trace *trace,
+                  char *err, size_t errlen)
 {
+	const bool vbm3d = (flags & BM4DOF_VBM3D_SEARCH) != 0;
 	if (!(C == 1 || C == 3 || C == 4))
 		return fail(err, errlen, "VideoNLB::runNlBayes: Wrong number of channels. Must be 1, 3 or 4.", BM4DOF_ERR_CHANNELS);
 	/* an empty forward flow disables flow (nldct.cpp:283); a forward flow
@@ -945,6 +1085,8 @@ int oracle_run(const float *noisy_in, const float *fflow_in, const float *bflow_
 			return fail(err, errlen, "oracle: unsupported parameters", BM4DOF_ERR_UNSUPPORTED);
 		if (p->doPasteBoost)
 			return fail(err, errlen, "oracle: doPasteBoost is not restated", BM4DOF_ERR_UNSUPPORTED);
+		if (vbm3d && p->nSimilarPatches > 1 && p->nSimilarPatchesPred == 0)
+			return fail(err, errlen, "oracle: nSimilarPatchesPred must be positive", BM4DOF_ERR_UNSUPPORTED);
 	}
 
 	Vid noisy(W, H, F, C);
@@ -986,7 +1128,7 @@ int oracle_run(const float *noisy_in, const float *fflow_in, const float *bflow_
 #endif
 		for (int n = 0; n < nt; n++)
 			cnt[n] = process_tile(nsub[n], fsub[n], bfsub[n], bsub[n], osub[n], p, crops[n],
-			                      trace ? &traces[s][n] : nullptr);
+			                      trace ? &traces[s][n] : nullptr, vbm3d);
 		if (s == 0) {
 			build_tight(bsub, basic, nparts, (int)p.boundary);
 			if (p.colorSpace == BM4DOF_YUV) color_transform(basic, false);
@@ -1016,6 +1158,15 @@ int oracle_run(const float *noisy_in, const float *fflow_in, const float *bflow_
 		trace->count = k;
 	}
 	return 0;
+}
+
+int oracle_run(const float *noisy_in, const float *fflow_in, const float *bflow_in,
+               unsigned W, unsigned H, unsigned C, unsigned F, float *basic_io, float *final_out,
+               const bm4dof_params *p1, const bm4dof_params *p2, unsigned nparts,
+               unsigned nthreads, float ratios[2], oracle_trace *trace, char *err, size_t errlen)
+{
+	return oracle_run_ex(noisy_in, fflow_in, bflow_in, W, H, C, F, basic_io, final_out, p1, p2,
+	                     nparts, nthreads, 0u, ratios, trace, err, errlen);
 }
 
 } // extern "C"

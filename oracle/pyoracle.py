@@ -18,6 +18,7 @@ REF_SO = os.path.join(HERE, "_ref", "libbm4dof_ref.so")
 # the reference built with its VBM3D_SEARCH switch (predictive patch search)
 REF_VBM3D_SO = os.path.join(HERE, "_ref", "libbm4dof_ref_vbm3d.so")
 REF_ROOT_DEFAULT = "/root/reference"
+VBM3D_SEARCH = 0x10   # BM4DOF_VBM3D_SEARCH of include/bm4dof.h
 
 
 class Params(C.Structure):
@@ -111,6 +112,9 @@ class Oracle(_Lib):
         L.oracle_run.restype = C.c_int
         L.oracle_run.argtypes = [C.POINTER(C.c_float)] * 3 + [C.c_uint] * 4 + [C.POINTER(C.c_float)] * 2 + \
             [C.POINTER(Params)] * 2 + [C.c_uint, C.c_uint, C.POINTER(C.c_float), C.POINTER(Trace), C.c_char_p, C.c_size_t]
+        L.oracle_run_ex.restype = C.c_int
+        L.oracle_run_ex.argtypes = [C.POINTER(C.c_float)] * 3 + [C.c_uint] * 4 + [C.POINTER(C.c_float)] * 2 + \
+            [C.POINTER(Params)] * 2 + [C.c_uint] * 3 + [C.POINTER(C.c_float), C.POINTER(Trace), C.c_char_p, C.c_size_t]
         L.oracle_basis.argtypes = [C.c_int, C.c_uint, C.c_uint, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.oracle_window.argtypes = [C.c_int, C.c_uint, C.c_uint, C.POINTER(C.c_float)]
         L.oracle_tile_crops.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_int, C.POINTER(C.c_int)]
@@ -119,8 +123,9 @@ class Oracle(_Lib):
         L.oracle_color_transform.argtypes = [C.POINTER(C.c_float), C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_int]
 
     def runNlBayes(self, noisy, fflow, bflow, p1, p2, basic=None, nparts=2, nthreads=1,
-                   trace_cap=0, trace_stride=16):
-        """noisy: (F, C, H, W) float32.  Returns (basic, final, ratios[, trace])."""
+                   trace_cap=0, trace_stride=16, vbm3d=False):
+        """noisy: (F, C, H, W) float32.  Returns (basic, final, ratios[, trace]).
+        vbm3d: the predictive search of the reference's VBM3D_SEARCH build."""
         noisy = np.ascontiguousarray(noisy, np.float32)
         F, Cc, H, W = noisy.shape
         fflow = None if fflow is None else np.ascontiguousarray(fflow, np.float32)
@@ -137,9 +142,9 @@ class Oracle(_Lib):
             up = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint))
             tr = Trace(trace_cap, trace_stride, up(arrays["step"]), up(arrays["tile"]), up(arrays["ref"]),
                        up(arrays["nsimp"]), up(arrays["index"]), 0)
-        rc = self.lib.oracle_run(_fp(noisy), _fp(fflow), _fp(bflow), W, H, Cc, F, _fp(b), _fp(fin),
-                                 C.byref(p1), C.byref(p2), nparts, nthreads, ratios,
-                                 C.byref(tr) if tr is not None else None, err, 512)
+        rc = self.lib.oracle_run_ex(_fp(noisy), _fp(fflow), _fp(bflow), W, H, Cc, F, _fp(b), _fp(fin),
+                                    C.byref(p1), C.byref(p2), nparts, nthreads, VBM3D_SEARCH if vbm3d else 0,
+                                    ratios, C.byref(tr) if tr is not None else None, err, 512)
         if rc:
             raise RuntimeError(err.value.decode())
         out = (b, fin, (ratios[0], ratios[1]))

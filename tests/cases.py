@@ -28,4 +28,13 @@ VBM3D_CASES = [
     ("vbm3d_video_4tiles", 44, 40, 6, 1, 30.0, 32, True, CFG_VIDEO, 2),
     ("vbm3d_noflow", 36, 32, 5, 1, 20.0, 33, False, CFG_VIDEO, 1),
     ("vbm3d_rgb", 30, 28, 4, 3, 20.0, 34, True, CFG_VIDEO, 1),
+    # the video defaults (8x8x1 patches, 7x7 window, 5x5 predicted windows,
+    # 2 matches per frame) over a 9-frame temporal range
+    ("vbm3d_defaults", 48, 40, 10, 1, 20.0, 35, True, {}, 1),
+    # 3 matches per frame, 7x7 predicted windows, no centre bias in step 2
+    ("vbm3d_npf3", 44, 36, 8, 1, 25.0, 36, True,
+     dict(px1=4, px2=4, pt1=2, pt2=2, wx1=15, wx2=13, np1=16, np2=16, npf1=3, npf2=3,
+          wxf1=7, wxf2=7, dsub2=0.0), 1),
+    # one frame: the whole search is the reference frame's window
+    ("vbm3d_image", 48, 40, 1, 1, 20.0, 37, False, CFG_IMAGE, 1),
 ]

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from cases import CASES
+from cases import CASES, VBM3D_CASES
 from helpers import ROOT, resolve_params, video_case
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -37,6 +37,27 @@ def test_oracle_matches_golden(oracle, case):
     assert np.array_equal(basic, g["basic"], equal_nan=True)
     assert np.array_equal(final, g["final"], equal_nan=True)
     assert ratios == tuple(g["ratios"].tolist())
+
+
+@pytest.mark.parametrize("case", VBM3D_CASES, ids=[c[0] for c in VBM3D_CASES])
+def test_oracle_vbm3d_matches_golden(oracle, case):
+    """The predictive search restatement against the reference's VBM3D_SEARCH build."""
+    g = load_case(case[0])
+    p1, p2 = params_from(oracle, g["p1"]), params_from(oracle, g["p2"])
+    nthreads = int(g["nthreads"])
+    basic, final, ratios = oracle.runNlBayes(g["noisy"], g.get("fflow"), g.get("bflow"), p1, p2,
+                                             nparts=2 * nthreads, nthreads=nthreads, vbm3d=True)
+    assert np.array_equal(basic, g["basic"], equal_nan=True)
+    assert np.array_equal(final, g["final"], equal_nan=True)
+    assert ratios == tuple(g["ratios"].tolist())
+
+
+def test_vbm3d_golden_differs_from_exhaustive(oracle):
+    """The predictive fixtures exercise a different neighbour search."""
+    g = load_case("vbm3d_video")
+    p1, p2 = params_from(oracle, g["p1"]), params_from(oracle, g["p2"])
+    basic, final, _ = oracle.runNlBayes(g["noisy"], g.get("fflow"), g.get("bflow"), p1, p2, nparts=2)
+    assert not np.array_equal(basic, g["basic"])
 
 
 def test_golden_denoises(oracle):
@@ -89,3 +110,19 @@ def test_errors_match_reference_messages(oracle, reference):
     with pytest.raises(RuntimeError) as b:
         reference.runNlBayes(nz, None, None, *pr)
     assert str(a.value) == str(b.value)
+
+
+@pytest.mark.parametrize("seed", [201, 202])
+def test_oracle_vbm3d_matches_reference_fresh(oracle, seed):
+    import pyoracle
+    if not pyoracle.Reference.available(pyoracle.REF_VBM3D_SO):
+        pytest.skip("reference sources not present (oracle/_ref not built)")
+    ref = pyoracle.Reference(pyoracle.REF_VBM3D_SO)
+    W, H, F = 38, 34, 7
+    clean, nz, ff, bf = video_case(W, H, F, sigma=25.0, seed=seed)
+    cfg = dict(px1=4, px2=4, pt1=1, pt2=2, wx1=11, wx2=9, np1=8, np2=16, npf1=2, npf2=4, wxf2=3)
+    po = resolve_params(oracle, (W, H, F, 1), 25.0, **cfg)
+    pr = resolve_params(ref, (W, H, F, 1), 25.0, **cfg)
+    a = oracle.runNlBayes(nz, ff, bf, *po, nparts=2, vbm3d=True)
+    b = ref.runNlBayes(nz, ff, bf, *pr, nthreads=1)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
