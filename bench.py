@@ -396,7 +396,7 @@ def main():
     forms = {}
     import train_gains
     gains = train_gains.load_weights()
-    variants = [("mixed", {"mixed": True})]
+    variants = [("mixed", {"mixed": True}), ("vbm3d_search", {"vbm3d": True})]
     if gains is not None:
         ctx.set_gain_network(gains)
         variants += [("learned", {"learned": True}), ("learned+mixed", {"learned": True, "mixed": True})]

@@ -24,6 +24,7 @@ DEVICE_POINTERS = 0x1
 KEEP_GROUPS = 0x2
 MIXED_PRECISION = 0x4
 LEARNED = 0x8
+VBM3D_SEARCH = 0x10   # the predictive search of the reference's VBM3D_SEARCH build
 GAIN_PARAMS = 99136   # floats in a gain-network parameter blob
 
 DCT, BIOR1_5 = 0, 1
@@ -226,11 +227,13 @@ def version() -> str:
 
 
 def cli_params(size, sigma, px1=-1, px2=-1, pt1=1, pt2=1, wx1=-1, wx2=-1, np1=-1, np2=-1, b1=-1.0,
-               b2=-1.0, bm1=-1.0, bm2=-1.0, no_step1=False, no_step2=False, order_inv=False, verbose=False):
+               b2=-1.0, bm1=-1.0, bm2=-1.0, no_step1=False, no_step2=False, order_inv=False, verbose=False,
+               wxf1=-1, wxf2=-1, npf1=-1, npf2=-1, dsub1=-1.0, dsub2=-1.0, t1=-1.0, t2=-1.0):
     """Parameters of both steps as the reference CLI resolves them from its
     flags (src/main_vnlb.cpp:206-246; -t1/-t2 only apply under VBM3D_SEARCH,
     -wt1/-wt2 never).  size = (width, height, frames, channels); -1 = flag
-    not given."""
+    not given.  wxf*/npf*/dsub*/t* are the options of the VBM3D_SEARCH build
+    (main_vnlb.cpp:227-236), for runs with vbm3d=True."""
     p1 = initializeNlbParameters(1, sigma, size, verbose)
     p2 = initializeNlbParameters(2, sigma, size, verbose)
     if wx1 >= 0: setSizeSearchWindow(p1, wx1)
@@ -247,6 +250,14 @@ def cli_params(size, sigma, px1=-1, px2=-1, pt1=1, pt2=1, wx1=-1, wx2=-1, np1=-1
     if pt2 >= 0: p2.sizePatchTime = pt2
     if no_step1: p1.offSet = 1
     if no_step2: p2.offSet = 1
+    if wxf1 >= 0: p1.sizeSearchWindowPred = wxf1
+    if wxf2 >= 0: p2.sizeSearchWindowPred = wxf2
+    if npf1 >= 0: p1.nSimilarPatchesPred = npf1
+    if npf2 >= 0: p2.nSimilarPatchesPred = npf2
+    if dsub1 >= 0: p1.dsub = dsub1
+    if dsub2 >= 0: p2.dsub = dsub2
+    if t1 >= 0: p1.tau = t1
+    if t2 >= 0: p2.tau = t2
     if order_inv:
         p1.orderInvariance = 1
         p2.orderInvariance = 1
@@ -279,15 +290,18 @@ class Context:
             pass
 
     def runNlBayes(self, noisy, fflow, bflow, p1, p2, basic=None, nparts=2, keep_groups=False,
-                   final=None, mixed=False, learned=False):
+                   final=None, mixed=False, learned=False, vbm3d=False):
         """VideoNLB::runNlBayes.  Returns (basic, final, (ratio1, ratio2)).
+
+        vbm3d=True searches neighbours like the reference built with
+        VBM3D_SEARCH (predictive search along the best matches of each frame).
 
         With CUDA tensors the inputs stay on the device and basic/final are
         CUDA tensors (pass preallocated ones to avoid allocation).
         learned=True runs the learned form (no step-1 pass; the gain network
         installed by set_gain_network, or none)."""
         flags = (KEEP_GROUPS if keep_groups else 0) | (MIXED_PRECISION if mixed else 0)
-        flags |= LEARNED if learned else 0
+        flags |= (LEARNED if learned else 0) | (VBM3D_SEARCH if vbm3d else 0)
         if _is_cuda_tensor(noisy):
             import torch
             F, Cc, H, W = noisy.shape
@@ -343,21 +357,21 @@ class Context:
             q.nparts = it.get("nparts", 2)
         return arr
 
-    def run_batched(self, items, mixed=False, learned=False, tuning=None):
+    def run_batched(self, items, mixed=False, learned=False, tuning=None, vbm3d=False):
         """Denoise many sequences with one CUDA graph (bm4dof_run_batched).
         Returns the per-sequence ratios."""
         arr = self._sequences(items)
-        flags = (MIXED_PRECISION if mixed else 0) | (LEARNED if learned else 0)
+        flags = (MIXED_PRECISION if mixed else 0) | (LEARNED if learned else 0) | (VBM3D_SEARCH if vbm3d else 0)
         t = None
         if tuning is not None:
             t = Tuning(**tuning) if isinstance(tuning, dict) else tuning
         _check(load().bm4dof_run_batched(self._h, arr, len(items), flags, C.byref(t) if t is not None else None))
         return [(q.ratios[0], q.ratios[1]) for q in arr]
 
-    def autotune(self, items, sample=16, mixed=False, learned=False):
+    def autotune(self, items, sample=16, mixed=False, learned=False, vbm3d=False):
         """(best tuning dict, table of (branches, slot_mb, search_ctas, ms))."""
         arr = self._sequences(items)
-        flags = (MIXED_PRECISION if mixed else 0) | (LEARNED if learned else 0)
+        flags = (MIXED_PRECISION if mixed else 0) | (LEARNED if learned else 0) | (VBM3D_SEARCH if vbm3d else 0)
         best = Tuning()
         table = (C.c_float * (4 * 32))()
         rows = C.c_uint()

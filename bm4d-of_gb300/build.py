@@ -24,7 +24,7 @@ CLI = os.path.join(OUT, "bm4dof")          # the command line, linked to LIB
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
-SOURCES = ["search.cu", "search_mixed.cu", "filter.cu", "aggregate.cu", "runtime.cu", "noalloc.cu",
+SOURCES = ["search.cu", "search_vbm3d.cu", "search_mixed.cu", "filter.cu", "aggregate.cu", "runtime.cu", "noalloc.cu",
            "mlp.cu", "learned.cu", "tvl1.cu",
            "params.cpp", "basis.cpp"]
 

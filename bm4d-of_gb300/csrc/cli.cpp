@@ -333,6 +333,27 @@ bool save_video(const std::string &pattern, unsigned first, unsigned step, const
 	return true;
 }
 
+// printNlbParameters (nldct.cpp:212-248); the predictive search adds three
+// lines to the patch-search block, as the reference's VBM3D_SEARCH build does.
+void print_params(const bm4dof_params &p, bool vbm3d)
+{
+	char buf[4096];
+	if (bm4dof_format_params(&p, buf, sizeof(buf)) <= 0) return;
+	std::string s(buf);
+	if (vbm3d) {
+		char extra[512];
+		const int wp = (int)p.sizeSearchWindowPred;
+		std::snprintf(extra, sizeof(extra),
+		              "\t\tPred. spatial search window = %dx%d\n"
+		              "\t\tPred. distance bias (dsub)  = %g\n"
+		              "\t\tSimilar patches per frame   = %d\n",
+		              wp, wp, p.dsub, (int)p.nSimilarPatchesPred);
+		const size_t at = s.find("\tGroup filtering:");
+		if (at != std::string::npos) s.insert(at, extra);
+	}
+	std::fputs(s.c_str(), stdout);
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -367,8 +388,9 @@ int main(int argc, char **argv)
 	const int patch_sizet2 = a.i("-pt2", 1, "< temporal patch size, step 2");
 	const int num_patches1 = a.i("-np1", -1, "< number of similar patches, step 1");
 	const int num_patches2 = a.i("-np2", -1, "< number of similar patches, step 2");
-	(void)a.f("-t1", -1.f, "< step 1 distance threshold");   // applies only to the VBM3D search build
-	(void)a.f("-t2", -1.f, "< step 2 distance threshold");
+	// -t1/-t2 apply to -print-prms always, to a run only with the predictive search
+	const float tau1 = a.f("-t1", -1.f, "< step 1 distance threshold");
+	const float tau2 = a.f("-t2", -1.f, "< step 2 distance threshold");
 	const float beta1 = a.f("-b1", -1.f, "< noise correction factor beta, step 1");
 	const float beta2 = a.f("-b2", -1.f, "< noise correction factor beta, step 2");
 	const float beta_mean1 = a.f("-bm1", -1.f, "< noise correction factor beta for mean, step 1");
@@ -382,6 +404,14 @@ int main(int argc, char **argv)
 	const unsigned nparts = (unsigned)a.i("-nparts", 2, "< spatial tiles (the reference: 2 x OpenMP threads)");
 	const int device = a.i("-device", 0, "< CUDA device");
 	const bool mixed = a.i("-mixed", 0, "< FP16 tensor-core distance pre-screen") != 0;
+	// the reference's VBM3D_SEARCH build as a run-time switch, with its options
+	const bool vbm3d = a.i("-vbm3d", 0, "< VBM3D predictive patch search") != 0;
+	const int space_search_f1 = a.i("-wxf1", -1, "< search window for predictive search, step 1");
+	const int space_search_f2 = a.i("-wxf2", -1, "< search window for predictive search, step 2");
+	const int num_patches_f1 = a.i("-npf1", -1, "< number of similar patches per frame, step 1");
+	const int num_patches_f2 = a.i("-npf2", -1, "< number of similar patches per frame, step 2");
+	const float dsub1 = a.f("-dsub1", -1.f, "< distance bias, step 1");
+	const float dsub2 = a.f("-dsub2", -1.f, "< distance bias, step 2");
 	(void)time_search1;
 	(void)time_search2;
 	if (a.help) return EXIT_SUCCESS;
@@ -467,10 +497,22 @@ int main(int argc, char **argv)
 	if (no_paste2) p2.doPasteBoost = 0;
 	if (no_step1) p1.offSet = 1;
 	if (no_step2) p2.offSet = 1;
+	if (vbm3d) {
+		if (space_search_f1 >= 0) p1.sizeSearchWindowPred = (unsigned)space_search_f1;
+		if (space_search_f2 >= 0) p2.sizeSearchWindowPred = (unsigned)space_search_f2;
+		if (num_patches_f1 >= 0) p1.nSimilarPatchesPred = (unsigned)num_patches_f1;
+		if (num_patches_f2 >= 0) p2.nSimilarPatchesPred = (unsigned)num_patches_f2;
+		if (dsub1 >= 0) p1.dsub = dsub1;
+		if (dsub2 >= 0) p2.dsub = dsub2;
+	}
+	if (print_prms || vbm3d) {
+		if (tau1 >= 0) p1.tau = tau1;
+		if (tau2 >= 0) p2.tau = tau2;
+	}
 	if (order_inv) p1.orderInvariance = p2.orderInvariance = 1;
 	if (print_prms) {
-		bm4dof_print_params(&p1);
-		bm4dof_print_params(&p2);
+		print_params(p1, vbm3d);
+		print_params(p2, vbm3d);
 		return EXIT_SUCCESS;
 	}
 
@@ -483,7 +525,8 @@ int main(int argc, char **argv)
 	const bm4dof_status s =
 	    bm4dof_run(ctx, noisy.data.data(), use_oflow ? fflow.data.data() : nullptr,
 	               use_oflow ? bflow.data.data() : nullptr, noisy.w, noisy.h, noisy.c, noisy.f, basic.data.data(),
-	               fin.data.data(), &p1, &p2, nparts, mixed ? BM4DOF_MIXED_PRECISION : 0u, ratios);
+	               fin.data.data(), &p1, &p2, nparts,
+	               (mixed ? BM4DOF_MIXED_PRECISION : 0u) | (vbm3d ? BM4DOF_VBM3D_SEARCH : 0u), ratios);
 	bm4dof_destroy(ctx);
 	if (s != BM4DOF_OK) return std::fprintf(stderr, "%s\n", bm4dof_last_error()), EXIT_FAILURE;
 	if (verbose)

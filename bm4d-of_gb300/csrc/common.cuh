@@ -52,6 +52,9 @@ struct StepParams {               // resolved parameters of one step
 	int search_ctas;              // exact search: CTAs per SM (4 or 6; 0 = default)
 	float beta_mean;              // betaMean (order-invariant filtering)
 	int order_inv;                // orderInvariance
+	int vbm3d;                    // predictive search (the reference's VBM3D_SEARCH build)
+	int wxp, npf;                 // sizeSearchWindowPred, nSimilarPatchesPred
+	float dsub_bias;              // dsub*dsub*255 (nldct.cpp:921)
 };
 
 // Locate the tile owning global group g (tiles are few: linear scan).

@@ -31,6 +31,13 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
                           const uint32_t *traj, const StepParams &sp, long long g_begin, long long g_end,
                           uint8_t *nsimp, uint32_t *idx, int *err, int nsm, cudaStream_t st);
 
+// search_vbm3d.cu (the reference's VBM3D_SEARCH build)
+bool vbm3d_check(const StepParams &sp, const std::vector<Tile> &tiles, std::string &why);
+size_t vbm3d_smem_bytes(const StepParams &sp, int reps);
+cudaError_t launch_search_vbm3d(const Image &src, const Image &ffl, const Image &bfl, const Tile *tiles,
+                                int ntiles, const int *grid, const StepParams &sp, int reps, long long g_begin,
+                                long long g_end, uint8_t *nsimp, uint32_t *idx, int nsm, cudaStream_t st);
+
 // search_mixed.cu
 void mixed_blocks(const std::vector<Tile> &tiles, std::vector<long long> &out);
 bool mixed_supported(const StepParams &sp);

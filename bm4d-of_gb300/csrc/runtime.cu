@@ -274,6 +274,7 @@ struct SampleOut {
 struct RunMode {
 	bool mixed = false;     // FP16 pre-screen search (+ BF16 transforms where built)
 	bool learned = false;   // learned form: groups searched on noisy, gain-network filter
+	bool vbm3d = false;     // predictive search of the reference's VBM3D_SEARCH build
 	float beta1 = 3.f;      // learned form: hard threshold of the non-mean rows
 	const SampleOut *samples = nullptr;   // training pairs instead of filtering
 };
@@ -411,6 +412,21 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	sp.search_ctas = ctx->search_ctas;
 	sp.beta_mean = p.betaMean;
 	sp.order_inv = p.orderInvariance ? 1 : 0;
+	sp.vbm3d = mode.vbm3d ? 1 : 0;
+	sp.wxp = (int)p.sizeSearchWindowPred;
+	sp.npf = (int)p.nSimilarPatchesPred;
+	sp.dsub_bias = p.dsub * p.dsub * 255.f;   // nldct.cpp:921, float
+	if (sp.vbm3d) {
+		std::string why;
+		if (!vbm3d_check(sp, pl.tiles, why)) {
+			set_error("bm4dof: predictive search: " + why);
+			return BM4DOF_ERR_UNSUPPORTED;
+		}
+		if (vbm3d_smem_bytes(sp, on_noisy ? 1 : (int)C) > (size_t)200 * 1024) {
+			set_error("bm4dof: predictive search: search windows too large");
+			return BM4DOF_ERR_UNSUPPORTED;
+		}
+	}
 	if ((mode.learned || mode.samples) && !learned_supported(sp)) {
 		set_error("bm4dof: the learned form needs grey video and 64-element patches");
 		return BM4DOF_ERR_UNSUPPORTED;
@@ -532,16 +548,23 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 	// ---- patch search of every group -------------------------------------
 	{
 		Mark m(ctx, T_SEARCH);
-		CK(launch_traj(ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp, G, S.d_traj, st));
-		if (S.mixed_search) {
+		if (sp.vbm3d) {
+			// trajectories are chained inside the search (they follow the matches)
+			CK(launch_search_vbm3d(on_noisy ? noisy : basic, ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp,
+			                       on_noisy ? 1 : (int)C, 0, G, S.d_nsimp, S.d_idx, ctx->nsm, st));
+			ctx->launches += 1;
+		} else if (S.mixed_search) {
 			// FP16 tensor-core pre-screen + exact re-rank of the best 2k
+			CK(launch_traj(ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp, G, S.d_traj, st));
 			CK(launch_search_mixed(on_noisy ? noisy : basic, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, S.d_blocks,
 			                       (long long)S.nblocks, S.d_nsimp, S.d_idx, ctx->nsm, st));
+			ctx->launches += 2;
 		} else {
+			CK(launch_traj(ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp, G, S.d_traj, st));
 			CK(launch_search(on_noisy ? noisy : basic, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, 0, G, S.d_nsimp,
 			                 S.d_idx, nullptr, ctx->nsm, st));
+			ctx->launches += 2;
 		}
-		ctx->launches += 2;
 	}
 
 	// ---- mask switch-offs (rare): killer -> victim edges, then fixed point --
@@ -836,8 +859,13 @@ bm4dof_status validate_run(RunArgs &r, const char *who)
 		return BM4DOF_ERR_NO_STEP;
 	}
 	if (r.step != 1 && !r.final_) { set_error(std::string(who) + ": final output is NULL"); return BM4DOF_ERR_ARGUMENT; }
-	if (r.flags & ~(BM4DOF_DEVICE_POINTERS | BM4DOF_KEEP_GROUPS | BM4DOF_MIXED_PRECISION | BM4DOF_LEARNED)) {
+	if (r.flags & ~(BM4DOF_DEVICE_POINTERS | BM4DOF_KEEP_GROUPS | BM4DOF_MIXED_PRECISION | BM4DOF_LEARNED |
+	                BM4DOF_VBM3D_SEARCH)) {
 		set_error(std::string(who) + ": unsupported flags");
+		return BM4DOF_ERR_UNSUPPORTED;
+	}
+	if ((r.flags & BM4DOF_VBM3D_SEARCH) && (r.flags & (BM4DOF_MIXED_PRECISION | BM4DOF_LEARNED))) {
+		set_error(std::string(who) + ": the predictive search runs on the plain FP32 path only");
 		return BM4DOF_ERR_UNSUPPORTED;
 	}
 	r.learned = (r.flags & BM4DOF_LEARNED) != 0;
@@ -855,6 +883,7 @@ bm4dof_status validate_run(RunArgs &r, const char *who)
 	r.keep = (r.flags & BM4DOF_KEEP_GROUPS) != 0;
 	r.mode = RunMode();
 	r.mode.mixed = (r.flags & BM4DOF_MIXED_PRECISION) != 0;
+	r.mode.vbm3d = (r.flags & BM4DOF_VBM3D_SEARCH) != 0;
 	r.mode.beta1 = r.p1.beta;
 	const bool color = r.C > 1;
 	r.yuv1 = color && r.p1.colorSpace == BM4DOF_YUV;
@@ -1207,7 +1236,7 @@ bm4dof_status bm4dof_run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigne
 		set_error("bm4dof_run_batched: null context or no sequences");
 		return BM4DOF_ERR_ARGUMENT;
 	}
-	if (flags & ~(BM4DOF_MIXED_PRECISION | BM4DOF_LEARNED | BM4DOF_DEVICE_POINTERS)) {
+	if (flags & ~(BM4DOF_MIXED_PRECISION | BM4DOF_LEARNED | BM4DOF_DEVICE_POINTERS | BM4DOF_VBM3D_SEARCH)) {
 		set_error("bm4dof_run_batched: unsupported flags");
 		return BM4DOF_ERR_UNSUPPORTED;
 	}

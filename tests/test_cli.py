@@ -70,6 +70,27 @@ def test_cli_print_params(cli, oracle):
     assert r.stdout == oracle.formatNlbParameters(p1) + oracle.formatNlbParameters(p2)
 
 
+def test_cli_print_params_tau(cli, oracle):
+    # -print-prms takes -t1/-t2 in every build (main_vnlb.cpp:173-174)
+    r = run(cli, "-i", "unused", "-print-prms", 1, "-sigma", 20, "-t1", 50, "-t2", 12.5)
+    assert r.returncode == 0
+    p1, p2 = resolve_params(oracle, (0, 0, 0, 1), 20.0, t1=50.0, t2=12.5)
+    assert r.stdout == oracle.formatNlbParameters(p1) + oracle.formatNlbParameters(p2)
+
+
+def test_cli_print_params_vbm3d(cli):
+    # -vbm3d prints what the reference built with VBM3D_SEARCH prints
+    import pyoracle
+    if not pyoracle.Reference.available(pyoracle.REF_VBM3D_SO):
+        pytest.skip("reference sources not present (oracle/_ref not built)")
+    ref = pyoracle.Reference(pyoracle.REF_VBM3D_SO)
+    r = run(cli, "-i", "unused", "-print-prms", 1, "-vbm3d", 1, "-sigma", 20, "-px1", 4, "-npf1", 3,
+            "-wxf2", 7, "-dsub2", 1.5, "-t1", 40)
+    assert r.returncode == 0
+    p1, p2 = resolve_params(ref, (0, 0, 0, 1), 20.0, px1=4, npf1=3, wxf2=7, dsub2=1.5, t1=40.0)
+    assert r.stdout == ref.formatNlbParameters(p1) + ref.formatNlbParameters(p2)
+
+
 def test_frame_formats_round_trip(tmp_path):
     rng = np.random.default_rng(0)
     a = rng.normal(0, 50, (3, 7, 5)).astype(np.float32)
@@ -103,3 +124,25 @@ def test_cli_matches_oracle(cli, gpulib, oracle, tmp_path):
             "-deno", tmp_path / "d_%03d.png", "-bsic", tmp_path / "s_%03d.png")
     assert r.returncode == 0, r.stderr[-2000:]
     assert (tmp_path / "d_001.png").read_bytes()[:8] == b"\x89PNG\r\n\x1a\n"
+
+
+@pytest.mark.gpu
+def test_cli_vbm3d_matches_oracle(cli, gpulib, oracle, tmp_path):
+    # -vbm3d: the predictive search, with its per-frame options and -t1
+    W, H, F, sigma = 44, 36, 6, 20.0
+    clean, nz, ff, bf = video_case(W, H, F, sigma=sigma, seed=32)
+    for t in range(F):
+        write_pfm(tmp_path / f"n_{t:03d}.pfm", nz[t])
+        write_flo(tmp_path / f"f_{t:03d}.flo", ff[t])
+        write_flo(tmp_path / f"b_{t:03d}.flo", bf[t])
+    r = run(cli, "-i", tmp_path / "n_%03d.pfm", "-fof", tmp_path / "f_%03d.flo", "-bof", tmp_path / "b_%03d.flo",
+            "-f", 0, "-l", F - 1, "-sigma", sigma, "-px1", 4, "-px2", 4, "-pt1", 2, "-pt2", 2, "-np1", 16,
+            "-np2", 16, "-wx1", 15, "-wx2", 15, "-vbm3d", 1, "-npf1", 3, "-wxf2", 7, "-t1", 60, "-verbose", 0,
+            "-deno", tmp_path / "d_%03d.pfm", "-bsic", tmp_path / "s_%03d.pfm")
+    assert r.returncode == 0, r.stderr[-2000:]
+    p1, p2 = resolve_params(oracle, (W, H, F, 1), sigma, px1=4, px2=4, pt1=2, pt2=2, np1=16, np2=16,
+                            wx1=15, wx2=15, npf1=3, wxf2=7, t1=60.0)
+    basic, final, _ = oracle.runNlBayes(nz, ff, bf, p1, p2, nparts=2, vbm3d=True)
+    got_f = np.stack([read_pfm(tmp_path / f"d_{t:03d}.pfm") for t in range(F)])
+    got_b = np.stack([read_pfm(tmp_path / f"s_{t:03d}.pfm") for t in range(F)])
+    assert np.array_equal(got_f, final) and np.array_equal(got_b, basic)
