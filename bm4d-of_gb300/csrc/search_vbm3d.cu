@@ -25,11 +25,12 @@
 // while the other warps of the SM hide its latency.  Frame pt's window is
 // computed in column strips (each row of the image loaded once for kR
 // vertically adjacent candidates); the predicted windows one candidate per
-// lane.  Selections: a warp bitonic sort (up to 64 candidates) or repeated
-// warp minima (more candidates) when the nearest are distinct, else an exact
-// replay of libstdc++'s heap selection by one lane.
+// lane.  Selections, when the nearest are distinct: repeated warp minima
+// (few nearest) or a warp bitonic sort (more nearest, up to 64 candidates);
+// else an exact replay of libstdc++'s heap selection by one lane.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "internal.hpp"
@@ -52,7 +53,8 @@ struct VArgs {
 	uint8_t *nsimp;
 	uint32_t *idx;
 	int reps;          // passes over channel 0: 1 in step 1, C in step 2
-	int cap_win;       // most candidates of one frame
+	int cap_win;       // most candidates of one frame (two predicted frames)
+	int cap_pred;      // most candidates of one predicted frame
 	int cap_pool;      // nSimilarPatchesPred * frames of the temporal range
 	int per_warp;      // floats of shared memory per warp
 };
@@ -107,17 +109,41 @@ __device__ __forceinline__ void warp_sort64(float &d0, int &i0, float &d1, int &
 		}
 }
 
+// Ascending sort of 32 (distance, position) pairs, one per lane.
+__device__ __forceinline__ void warp_sort32(float &d0, int &i0)
+{
+	const int lane = threadIdx.x & 31;
+#pragma unroll
+	for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+		for (int j = k >> 1; j > 0; j >>= 1) {
+			const float od = __shfl_xor_sync(kFull, d0, j);
+			const int oi = __shfl_xor_sync(kFull, i0, j);
+			const bool low = (lane & j) == 0, up = (lane & k) == 0;
+			const bool take = (low == up) ? lex_less(od, oi, d0, i0) : lex_less(d0, i0, od, oi);
+			if (take) { d0 = od; i0 = oi; }
+		}
+}
+
+constexpr int kRoundsMaxK = 5;   // repeated minima up to this K, else a bitonic sort
+
 // The K nearest of d[0..n) (1 <= K <= min(n, kMaxNp)) in the order
 // std::partial_sort(d, d + K, d + n) leaves them: distances to od[0..K),
-// positions in d to oi[0..K).  Called by all 32 lanes of a warp.
-__device__ void warp_partial_sort(const float *d, int n, int K, float *od, int *oi, float *hd, int *hi)
+// positions in d to oi[0..K).  `nan`: this lane saw a NaN among the
+// distances.  Called by all 32 lanes of a warp.
+__device__ void warp_partial_sort(const float *d, int n, int K, bool nan, float *od, int *oi, float *hd, int *hi)
 {
 	const int lane = threadIdx.x & 31;
 	const float inf = __int_as_float(0x7f800000);
-	bool nan = false;
-	for (int i = lane; i < n; i += 32) nan |= d[i] != d[i];
 	bool ok = !__any_sync(kFull, nan);
-	if (ok && n <= 64) {
+	if (ok && n <= 32 && K > kRoundsMaxK) {
+		float d0 = lane < n ? d[lane] : inf;
+		int i0 = lane < n ? lane : 0x7fffffff;
+		warp_sort32(d0, i0);
+		const float next = __shfl_down_sync(kFull, d0, 1);
+		ok = !__any_sync(kFull, lane < K && lane + 1 < n && next == d0);
+		if (ok && lane < K) { od[lane] = d0; oi[lane] = i0; }
+	} else if (ok && n <= 64 && K > kRoundsMaxK) {
 		float d0 = lane < n ? d[lane] : inf, d1 = lane + 32 < n ? d[lane + 32] : inf;
 		int i0 = lane < n ? lane : 0x7fffffff, i1 = lane + 32 < n ? lane + 32 : 0x7fffffff;
 		warp_sort64(d0, i0, d1, i1);
@@ -187,18 +213,58 @@ __device__ void warp_partial_sort(const float *d, int n, int K, float *od, int *
 	__syncwarp();
 }
 
-// Squared distance of the reference patch (ref, `reps` copies of channel 0
-// at stride spc) to the patch at p (channel 0 of the candidate's first row
-// and frame), terms in the reference's order.
+// One half-warp's selection (lanes 16h .. 16h+15, both halves call it
+// together, each on its own frame): the K nearest of d[0..n) by K + 1 rounds
+// of the half's minimum over (distance, position), valid when they are
+// pairwise distinct and strictly below the rest.  Returns false on the
+// half's lanes when a tie or a NaN (`nan`: this lane saw one) leaves the
+// order to partial_sort's heap mechanics.
+__device__ bool half_select(const float *d, int n, int K, bool nan, float *od, int *oi)
+{
+	const int hl = threadIdx.x & 15;
+	const float inf = __int_as_float(0x7f800000);
+	const unsigned nm = __ballot_sync(kFull, nan);
+	bool ok = ((nm >> (threadIdx.x & 16)) & 0xffffu) == 0u;
+	float pv = -inf;
+	int pi = -1;
+	for (int r = 0; r <= K; r++) {
+		float bv = inf;
+		int bi = 0x7fffffff;
+		for (int i = hl; i < n; i += 16) {
+			const float v = d[i];
+			if (lex_less(pv, pi, v, i) && lex_less(v, i, bv, bi)) { bv = v; bi = i; }
+		}
+#pragma unroll
+		for (int o = 8; o > 0; o >>= 1) {
+			const float ov = __shfl_xor_sync(kFull, bv, o);
+			const int oi2 = __shfl_xor_sync(kFull, bi, o);
+			if (lex_less(ov, oi2, bv, bi)) { bv = ov; bi = oi2; }
+		}
+		if (r > 0 && r < n && !(bv > pv)) ok = false;
+		if (ok && r < K && hl == 0) { od[r] = bv; oi[r] = bi; }
+		pv = bv;
+		pi = bi;
+	}
+	__syncwarp();
+	return ok;
+}
+
+// Squared distances of the reference patch (ref, `reps` copies of channel 0
+// at stride spc) to the patches at p0 and p1 (channel 0 of each candidate's
+// first row and frame), terms in the reference's order; the two sums run
+// interleaved so that each hides the other's add latency.
 template <int PX, int PT>
-__device__ __forceinline__ float patch_distance(const float *p, size_t rpitch, size_t tpitch, const float *ref,
-                                                int reps, int px_rt, int pt_rt)
+__device__ __forceinline__ void patch_distance2(const float *p0, const float *p1, size_t rpitch, size_t tpitch,
+                                                const float *ref, int reps, int px_rt, int pt_rt, float &a0,
+                                                float &a1)
 {
 	const int px = PX > 0 ? PX : px_rt, pt = PX > 0 ? PT : pt_rt, spc = px * px * pt;
-	float acc = 0.f;
+	a0 = 0.f;
+	a1 = 0.f;
 	for (int r = 0; r < reps; r++) {
 		const float *rr = ref + r * spc;
-#pragma unroll
+		// one patch frame unrolled at a time (bounded register use)
+#pragma unroll 1
 		for (int ht = 0; ht < (PX > 0 ? PT : 1); ht++) {
 			for (int ht2 = 0; ht2 < (PX > 0 ? 1 : pt); ht2++) {
 				const int tt = PX > 0 ? ht : ht2;
@@ -206,14 +272,30 @@ __device__ __forceinline__ float patch_distance(const float *p, size_t rpitch, s
 				for (int hy = 0; hy < (PX > 0 ? PX : 1); hy++) {
 					for (int hy2 = 0; hy2 < (PX > 0 ? 1 : px); hy2++) {
 						const int yy = PX > 0 ? hy : hy2;
-						const float *row = p + tt * tpitch + yy * rpitch;
+						const size_t off = tt * tpitch + yy * rpitch;
 						const float *rf = rr + (tt * px + yy) * px;
+						// the reference row from shared memory in 16-byte loads
+						constexpr int QV = (PX > 0 && PX % 4 == 0) ? PX : 4;
+						float rrow[QV];
+						if (PX > 0 && PX % 4 == 0) {
+#pragma unroll
+							for (int q = 0; q < QV / 4; q++) {
+								const float4 r4 = reinterpret_cast<const float4 *>(rf)[q];
+								rrow[4 * q] = r4.x;
+								rrow[4 * q + 1] = r4.y;
+								rrow[4 * q + 2] = r4.z;
+								rrow[4 * q + 3] = r4.w;
+							}
+						}
 #pragma unroll
 						for (int hx = 0; hx < (PX > 0 ? PX : 1); hx++) {
 							for (int hx2 = 0; hx2 < (PX > 0 ? 1 : px); hx2++) {
 								const int xx = PX > 0 ? hx : hx2;
-								const float df = __fsub_rn(rf[xx], __ldg(row + xx));
-								acc = __fadd_rn(acc, __fmul_rn(df, df));
+								const float rv = (PX > 0 && PX % 4 == 0) ? rrow[xx % QV] : rf[xx];
+								const float d0 = __fsub_rn(rv, __ldg(p0 + off + xx));
+								const float d1 = __fsub_rn(rv, __ldg(p1 + off + xx));
+								a0 = __fadd_rn(a0, __fmul_rn(d0, d0));
+								a1 = __fadd_rn(a1, __fmul_rn(d1, d1));
 							}
 						}
 					}
@@ -221,7 +303,6 @@ __device__ __forceinline__ float patch_distance(const float *p, size_t rpitch, s
 			}
 		}
 	}
-	return acc;
 }
 
 // Window of one centre, shifted (not clipped) into the frame
@@ -238,8 +319,8 @@ __device__ __forceinline__ void window_box(int cx, int cy, int sw, int tw, int t
 	ny = max(0, min(th - px, cy + hw - shy) - y0 + 1);
 }
 
-template <int PX, int PT>
-__global__ void __launch_bounds__(32 * kWarps)
+template <int PX, int PT, int MINB>
+__global__ void __launch_bounds__(32 * kWarps, MINB)
 search_vbm3d_kernel(Image src, Image ffl, Image bfl, StepParams sp, VArgs a)
 {
 	extern __shared__ __align__(16) float smem_v[];
@@ -274,15 +355,20 @@ search_vbm3d_kernel(Image src, Image ffl, Image bfl, StepParams sp, VArgs a)
 			ref[k] = src.p[src.at(T.ox + x + hx, T.oy + y + hy, t + ht, 0)];
 		}
 		__syncwarp();
-		for (int ii = 0; ii < nwt; ii++) {
+		// with at most 16 matches per frame the forward and backward frames run
+		// in pairs, one per half-warp (below); else one frame at a time here
+		const bool paired = npf <= 16;
+		for (int ii = 0; ii < (paired ? 1 : nwt); ii++) {
 			const int qt = visit_frame(ii, t, t1);
 			int ncand, fx0 = 0, fy0 = 0, fnx = 1;
+			bool nan;
 			if (ii == 0) {
 				// frame pt: one full window, column strips of kR candidates
 				int fny;
 				window_box(x, y, sp.wx, T.w, T.h, px, fx0, fy0, fnx, fny);
 				ncand = fnx * fny;
 				const int nit = fnx * ((fny + kR - 1) / kR);
+				nan = false;
 				for (int it = lane; it < nit; it += 32) {
 					const int rb = it / fnx, cx = it - rb * fnx, qy0 = rb * kR;
 					float acc[kR];
@@ -294,6 +380,7 @@ search_vbm3d_kernel(Image src, Image ffl, Image bfl, StepParams sp, VArgs a)
 						if (qy0 + r < fny) {
 							float dv = acc[r];
 							if (fx0 + cx == x && fy0 + qy0 + r == y) dv = __fsub_rn(dv, sp.dsub_bias);
+							nan |= dv != dv;
 							dist[(qy0 + r) * fnx + cx] = dv;
 						}
 				}
@@ -338,18 +425,30 @@ search_vbm3d_kernel(Image src, Image ffl, Image bfl, StepParams sp, VArgs a)
 					}
 				}
 				__syncwarp();
-				for (int c = lane; c < ncand; c += 32) {
-					const uint32_t q = pos[c];
-					const int qx = (int)(q & 0xffffu), qy = (int)(q >> 16);
-					float dv = patch_distance<PX, PT>(src.p + src.at(T.ox + qx, T.oy + qy, qt, 0), rpitch, tpitch,
-					                                  ref, a.reps, px, sp.pt);
-					if (qx == x && qy == y) dv = __fsub_rn(dv, sp.dsub_bias);
-					dist[c] = dv;
+				nan = false;
+				// candidates c and c + 32 of a lane computed together
+				for (int c = lane; c < ncand; c += 64) {
+					const bool two = c + 32 < ncand;
+					const uint32_t q0 = pos[c], q1 = two ? pos[c + 32] : q0;
+					const int qx0 = (int)(q0 & 0xffffu), qy0 = (int)(q0 >> 16);
+					const int qx1 = (int)(q1 & 0xffffu), qy1 = (int)(q1 >> 16);
+					float d0, d1;
+					patch_distance2<PX, PT>(src.p + src.at(T.ox + qx0, T.oy + qy0, qt, 0),
+					                        src.p + src.at(T.ox + qx1, T.oy + qy1, qt, 0), rpitch, tpitch, ref,
+					                        a.reps, px, sp.pt, d0, d1);
+					if (qx0 == x && qy0 == y) d0 = __fsub_rn(d0, sp.dsub_bias);
+					if (qx1 == x && qy1 == y) d1 = __fsub_rn(d1, sp.dsub_bias);
+					nan |= d0 != d0;
+					dist[c] = d0;
+					if (two) {
+						nan |= d1 != d1;
+						dist[c + 32] = d1;
+					}
 				}
 			}
 			__syncwarp();
 			// the npf nearest of this frame join the pool, in partial_sort order
-			warp_partial_sort(dist, ncand, npf, sel_d, sel_i, hd, hi);
+			warp_partial_sort(dist, ncand, npf, nan, sel_d, sel_i, hd, hi);
 			if (lane < npf) {
 				const int c = sel_i[lane];
 				int qx, qy;
@@ -366,10 +465,114 @@ search_vbm3d_kernel(Image src, Image ffl, Image bfl, StepParams sp, VArgs a)
 			}
 			__syncwarp();
 		}
+		if (paired) {
+			// forward frame t + k on lanes 0-15 and backward frame t - k on lanes
+			// 16-31: centres, union lists and selections side by side, distances
+			// over both lists with the whole warp; pool slots in visiting order
+			const int nf = t1 - t, nb = t - t0;
+			const int h = lane >> 4, hl = lane & 15;
+			const int kmax = nf > nb ? nf : nb;
+			uint32_t *hpos = pos + h * a.cap_pred;
+			float *hdist = dist + h * a.cap_pred;
+			for (int k = 1; k <= kmax; k++) {
+				const bool act = h == 0 ? k <= nf : k <= nb;
+				const int dir = h == 0 ? 1 : -1;
+				const int qt = t + dir * k;
+				const int slot = h == 0 ? k : nf + k;
+				const int prev = h == 0 ? k - 1 : (k == 1 ? 0 : nf + k - 1);
+				int bx0 = 0, by0 = 0, bnx = 0, bny = 0;
+				if (act && hl < npf) {
+					const uint32_t id = pool_i[prev * npf + hl];
+					const int cx0 = (int)(id % (uint32_t)T.w);
+					const int cy0 = (int)((id / (uint32_t)T.w) % (uint32_t)T.h);
+					const int ct0 = qt - dir;
+					float ux = 0.f, uy = 0.f;
+					if (sp.use_flow) {
+						const Image &fl = dir > 0 ? ffl : bfl;
+						ux = fl.p[fl.at(T.ox + cx0, T.oy + cy0, ct0, 0)];
+						uy = fl.p[fl.at(T.ox + cx0, T.oy + cy0, ct0, 1)];
+					}
+					const int cx = (int)fmaxf(0.f, fminf(__fsub_rn((float)T.w, 1.f), roundf(__fadd_rn((float)cx0, ux))));
+					const int cy = (int)fmaxf(0.f, fminf(__fsub_rn((float)T.h, 1.f), roundf(__fadd_rn((float)cy0, uy))));
+					window_box(cx, cy, sp.wxp, T.w, T.h, px, bx0, by0, bnx, bny);
+				}
+				// each half's union, 16 positions per ballot
+				int cnt = 0;
+				for (int w = 0; w < npf; w++) {
+					const int sl = (h << 4) + w;
+					const int wx0 = __shfl_sync(kFull, bx0, sl), wy0 = __shfl_sync(kFull, by0, sl);
+					const int wnx = __shfl_sync(kFull, bnx, sl), wny = __shfl_sync(kFull, bny, sl);
+					const int nbw = wnx * wny;
+					const int nbo = __shfl_xor_sync(kFull, nbw, 16);
+					const int nbmax = nbw > nbo ? nbw : nbo;
+					for (int base = 0; base < nbmax; base += 16) {
+						const int p = base + hl;
+						const bool in = p < nbw;
+						const int qx = in ? wx0 + p % wnx : 0, qy = in ? wy0 + p / wnx : 0;
+						bool fresh = in;
+						for (int o = 0; o < w; o++) {
+							const int so = (h << 4) + o;
+							const int ox0 = __shfl_sync(kFull, bx0, so), oy0 = __shfl_sync(kFull, by0, so);
+							const int onx = __shfl_sync(kFull, bnx, so), ony = __shfl_sync(kFull, bny, so);
+							if (qx >= ox0 && qx < ox0 + onx && qy >= oy0 && qy < oy0 + ony) fresh = false;
+						}
+						const unsigned m = (__ballot_sync(kFull, fresh) >> (h << 4)) & 0xffffu;
+						if (fresh) hpos[cnt + __popc(m & ((1u << hl) - 1u))] = (uint32_t)qx | ((uint32_t)qy << 16);
+						cnt += __popc(m);
+					}
+				}
+				const int nF = __shfl_sync(kFull, cnt, 0), nB = __shfl_sync(kFull, cnt, 16);
+				__syncwarp();
+				// distances of both lists, candidates c and c + 32 of a lane together
+				bool nanF = false, nanB = false;
+				const int ntot = nF + nB;
+				for (int c = lane; c < ntot; c += 64) {
+					const bool two = c + 32 < ntot;
+					const int c1 = two ? c + 32 : c;
+					const int s0 = c < nF ? 0 : 1, s1 = c1 < nF ? 0 : 1;
+					const int j0 = c - s0 * nF, j1 = c1 - s1 * nF;
+					const uint32_t q0 = pos[s0 * a.cap_pred + j0], q1 = pos[s1 * a.cap_pred + j1];
+					const int qx0 = (int)(q0 & 0xffffu), qy0 = (int)(q0 >> 16);
+					const int qx1 = (int)(q1 & 0xffffu), qy1 = (int)(q1 >> 16);
+					float d0, d1;
+					patch_distance2<PX, PT>(src.p + src.at(T.ox + qx0, T.oy + qy0, s0 ? t - k : t + k, 0),
+					                        src.p + src.at(T.ox + qx1, T.oy + qy1, s1 ? t - k : t + k, 0), rpitch,
+					                        tpitch, ref, a.reps, px, sp.pt, d0, d1);
+					if (qx0 == x && qy0 == y) d0 = __fsub_rn(d0, sp.dsub_bias);
+					if (qx1 == x && qy1 == y) d1 = __fsub_rn(d1, sp.dsub_bias);
+					dist[s0 * a.cap_pred + j0] = d0;
+					if (s0) nanB |= d0 != d0; else nanF |= d0 != d0;
+					if (two) {
+						dist[s1 * a.cap_pred + j1] = d1;
+						if (s1) nanB |= d1 != d1; else nanF |= d1 != d1;
+					}
+				}
+				__syncwarp();
+				const int nh = h == 0 ? nF : nB;
+				float *hsd = sel_d + (h << 4);
+				int *hsi = sel_i + (h << 4);
+				const bool fnan = __any_sync(kFull, nanF), bnan = __any_sync(kFull, nanB);
+				const bool ok = half_select(hdist, nh, npf, h == 0 ? fnan : bnan, hsd, hsi) || !act;
+				// ties or NaN: libstdc++'s heap selection replayed for that frame
+				const unsigned bad = __ballot_sync(kFull, !ok);
+				if (bad & 0xffffu) warp_partial_sort(dist, nF, npf, true, sel_d, sel_i, hd, hi);
+				if (bad & 0xffff0000u)
+					warp_partial_sort(dist + a.cap_pred, nB, npf, true, sel_d + 16, sel_i + 16, hd, hi);
+				if (act && hl < npf) {
+					const uint32_t q = hpos[hsi[hl]];
+					const int qx = (int)(q & 0xffffu), qy = (int)(q >> 16);
+					pool_d[slot * npf + hl] = hsd[hl];
+					pool_i[slot * npf + hl] = (uint32_t)(((long long)qt * T.h + qy) * T.w + qx);
+				}
+				__syncwarp();
+			}
+		}
 		// the np nearest of the pool, then the tau rule (nldct.cpp:1075-1104)
 		const int npool = nwt * npf;
 		const int K = min(sp.np, npool);
-		warp_partial_sort(pool_d, npool, K, sel_d, sel_i, hd, hi);
+		bool pnan = false;
+		for (int i = lane; i < npool; i += 32) pnan |= pool_d[i] != pool_d[i];
+		warp_partial_sort(pool_d, npool, K, pnan, sel_d, sel_i, hd, hi);
 		int n = 1;
 		while (2 * n <= K && sel_d[n] < sp.tau2) n *= 2;
 		if (lane == 0) a.nsimp[g] = (uint8_t)n;
@@ -378,11 +581,11 @@ search_vbm3d_kernel(Image src, Image ffl, Image bfl, StepParams sp, VArgs a)
 	}
 }
 
-template <int PX, int PT>
+template <int PX, int PT, int MINB = 1>
 cudaError_t launch_t(const Image &src, const Image &ffl, const Image &bfl, const StepParams &sp, const VArgs &a,
                      int nsm, cudaStream_t st)
 {
-	auto kern = search_vbm3d_kernel<PX, PT>;
+	auto kern = search_vbm3d_kernel<PX, PT, MINB>;
 	const size_t smem = sizeof(float) * (size_t)a.per_warp * kWarps;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
@@ -428,7 +631,7 @@ bool vbm3d_check(const StepParams &sp, const std::vector<Tile> &tiles, std::stri
 size_t vbm3d_smem_bytes(const StepParams &sp, int reps)
 {
 	const int hw = 2 * ((sp.wx - 1) / 2) + 1, hp = 2 * ((sp.wxp - 1) / 2) + 1;
-	const int cap_win = hw * hw > sp.npf * hp * hp ? hw * hw : sp.npf * hp * hp;
+	const int cap_win = hw * hw > 2 * sp.npf * hp * hp ? hw * hw : 2 * sp.npf * hp * hp;
 	const Layout lo(reps, sp.spc, cap_win, sp.npf * search_frames_max(sp));
 	return sizeof(float) * (size_t)lo.total * kWarps;
 }
@@ -450,11 +653,22 @@ cudaError_t launch_search_vbm3d(const Image &src, const Image &ffl, const Image 
 	a.idx = idx;
 	a.reps = reps;
 	const int hw = 2 * ((sp.wx - 1) / 2) + 1, hp = 2 * ((sp.wxp - 1) / 2) + 1;
-	a.cap_win = hw * hw > sp.npf * hp * hp ? hw * hw : sp.npf * hp * hp;
+	a.cap_pred = sp.npf * hp * hp;
+	a.cap_win = hw * hw > 2 * a.cap_pred ? hw * hw : 2 * a.cap_pred;
 	a.cap_pool = sp.npf * search_frames_max(sp);
 	a.per_warp = Layout(reps, sp.spc, a.cap_win, a.cap_pool).total;
-	if (sp.px == 4 && sp.pt == 4) return launch_t<4, 4>(src, ffl, bfl, sp, a, nsm, st);
-	if (sp.px == 8 && sp.pt == 1) return launch_t<8, 1>(src, ffl, bfl, sp, a, nsm, st);
+	// CTAs per SM for 4x4x4 patches (registers bound the occupancy of this
+	// latency-bound kernel); BM4DOF_VBM3D_MINB selects 4, 6 or 8
+	static const int minb = [] {
+		const char *e = std::getenv("BM4DOF_VBM3D_MINB");
+		return e ? std::atoi(e) : 8;
+	}();
+	if (sp.px == 4 && sp.pt == 4) {
+		if (minb == 4) return launch_t<4, 4, 4>(src, ffl, bfl, sp, a, nsm, st);
+		if (minb == 6) return launch_t<4, 4, 6>(src, ffl, bfl, sp, a, nsm, st);
+		return launch_t<4, 4, 8>(src, ffl, bfl, sp, a, nsm, st);
+	}
+	if (sp.px == 8 && sp.pt == 1) return launch_t<8, 1, 4>(src, ffl, bfl, sp, a, nsm, st);
 	return launch_t<0, 0>(src, ffl, bfl, sp, a, nsm, st);
 }
 
