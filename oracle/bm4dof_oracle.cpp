@@ -964,11 +964,27 @@ unsigned process_tile(const Vid &noisy, const Vid &fflow, const Vid &bflow, Vid 
 									weight.d[ind1 + qt * wh + qy * W + qx] += aggw[n] * w.win[i];
 					}
 				}
-				/* mask(index[0]) = false, nldct.cpp:2325-2329: the index carries the
-				 * channel stride, so for C > 1 it addresses another frame of the
-				 * one-channel mask; writes past the mask are skipped here (the
-				 * reference writes out of bounds there). */
-				if ((size_t)index[0] < mask.size()) mask[index[0]] = 0;
+				if (p.doPasteBoost) {
+					/* paste trick, nldct.cpp:2302-2322 / 2395-2415: every member's
+					 * position and its four neighbours away from the border band
+					 * of 2*sPx (unsigned comparisons, as the reference's) */
+					for (unsigned n = 0; n < nS; n++) {
+						const unsigned ind = index[n];
+						const unsigned ind1 = (ind / whc) * wh + ind % wh;
+						const unsigned mx = ind1 % W, my = (ind1 / W) % H;
+						mask[ind1] = 0;
+						if (my > 2 * sPx) mask[ind1 - W] = 0;
+						if (my < H - 2 * sPx) mask[ind1 + W] = 0;
+						if (mx > 2 * sPx) mask[ind1 - 1] = 0;
+						if (mx < W - 2 * sPx) mask[ind1 + 1] = 0;
+					}
+				} else {
+					/* mask(index[0]) = false, nldct.cpp:2325-2329: the index carries
+					 * the channel stride, so for C > 1 it addresses another frame of
+					 * the one-channel mask; writes past the mask are skipped here
+					 * (the reference writes out of bounds there). */
+					if ((size_t)index[0] < mask.size()) mask[index[0]] = 0;
+				}
 			}
 
 	/* computeWeightedAggregation, nldct.cpp:2436-2448 */
@@ -1083,8 +1099,6 @@ int oracle_run_ex(const float *noisy_in, const float *fflow_in, const float *bfl
 			return fail(err, errlen, "VideoNLB::processNlBayes: bior1_5 transform is only implemented for patches of size 8 x 8 x pt.", BM4DOF_ERR_BIOR_SIZE);
 		if (p->offSet == 0 || p->offSetTime == 0 || p->sizePatchTime == 0)
 			return fail(err, errlen, "oracle: unsupported parameters", BM4DOF_ERR_UNSUPPORTED);
-		if (p->doPasteBoost)
-			return fail(err, errlen, "oracle: doPasteBoost is not restated", BM4DOF_ERR_UNSUPPORTED);
 		if (vbm3d && p->nSimilarPatches > 1 && p->nSimilarPatchesPred == 0)
 			return fail(err, errlen, "oracle: nSimilarPatchesPred must be positive", BM4DOF_ERR_UNSUPPORTED);
 	}

@@ -18,6 +18,11 @@ CASES = [
     # -order-inv: one Wiener gain per coefficient for the mean row and one for the rest
     ("video_order_inv", 40, 36, 6, 1, 20.0, 21, True, dict(CFG_VIDEO, order_inv=True), 1),
     ("image_order_inv", 48, 40, 1, 1, 25.0, 22, False, dict(CFG_IMAGE, order_inv=True), 1),
+    # doPasteBoost: every member's position and its 4 neighbours leave the mask
+    ("video_paste", 40, 36, 6, 1, 20.0, 23, True, dict(CFG_VIDEO, paste_boost=True), 1),
+    ("video_paste_4tiles", 44, 40, 6, 1, 20.0, 24, True, dict(CFG_VIDEO, paste_boost=True), 2),
+    ("image_paste", 48, 40, 1, 1, 20.0, 25, False, dict(CFG_IMAGE, paste_boost=True), 1),
+    ("rgb_video_paste", 30, 28, 4, 3, 20.0, 26, True, dict(CFG_VIDEO, paste_boost=True), 1),
 ]
 
 # The reference built with its VBM3D_SEARCH switch: predictive search (the
@@ -37,4 +42,5 @@ VBM3D_CASES = [
           wxf1=7, wxf2=7, dsub2=0.0), 1),
     # one frame: the whole search is the reference frame's window
     ("vbm3d_image", 48, 40, 1, 1, 20.0, 37, False, CFG_IMAGE, 1),
+    ("vbm3d_paste", 40, 36, 6, 1, 20.0, 38, True, dict(CFG_VIDEO, paste_boost=True), 1),
 ]

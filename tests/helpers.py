@@ -19,10 +19,11 @@ import synthetic  # noqa: E402
 def resolve_params(lib, size, sigma, px1=-1, px2=-1, pt1=1, pt2=1, wx1=-1, wx2=-1,
                    np1=-1, np2=-1, b1=-1.0, b2=-1.0, bm1=-1.0, bm2=-1.0, no_step1=False,
                    no_step2=False, order_inv=False, verbose=False, wxf1=-1, wxf2=-1, npf1=-1,
-                   npf2=-1, dsub1=-1.0, dsub2=-1.0, t1=-1.0, t2=-1.0):
+                   npf2=-1, dsub1=-1.0, dsub2=-1.0, t1=-1.0, t2=-1.0, paste_boost=False):
     """Parameter resolution of the reference CLI, src/main_vnlb.cpp:206-246
     (the run path: -t1/-t2 only apply under VBM3D_SEARCH, -wt1/-wt2 never).
-    wxf*/npf*/dsub*/t* are the VBM3D_SEARCH build's options (main_vnlb.cpp:227-236)."""
+    wxf*/npf*/dsub*/t* are the VBM3D_SEARCH build's options (main_vnlb.cpp:227-236).
+    paste_boost sets nlbParams::doPasteBoost in both steps (no CLI flag enables it)."""
     p1 = lib.initializeNlbParameters(1, sigma, size, verbose)
     p2 = lib.initializeNlbParameters(2, sigma, size, verbose)
     if wx1 >= 0: lib.setSizeSearchWindow(p1, wx1)
@@ -50,6 +51,9 @@ def resolve_params(lib, size, sigma, px1=-1, px2=-1, pt1=1, pt2=1, wx1=-1, wx2=-
     if order_inv:
         p1.orderInvariance = 1
         p2.orderInvariance = 1
+    if paste_boost:
+        p1.doPasteBoost = 1
+        p2.doPasteBoost = 1
     return p1, p2
 
 

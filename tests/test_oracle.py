@@ -126,3 +126,16 @@ def test_oracle_vbm3d_matches_reference_fresh(oracle, seed):
     a = oracle.runNlBayes(nz, ff, bf, *po, nparts=2, vbm3d=True)
     b = ref.runNlBayes(nz, ff, bf, *pr, nthreads=1)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
+
+
+@pytest.mark.parametrize("seed", [211, 212])
+def test_oracle_paste_boost_matches_reference_fresh(oracle, reference, seed):
+    """doPasteBoost (reachable through the API only) against the compiled reference."""
+    from cases import CFG_VIDEO
+    W, H, F = 42, 34, 6
+    clean, nz, ff, bf = video_case(W, H, F, sigma=25.0, seed=seed)
+    po = resolve_params(oracle, (W, H, F, 1), 25.0, paste_boost=True, **CFG_VIDEO)
+    pr = resolve_params(reference, (W, H, F, 1), 25.0, paste_boost=True, **CFG_VIDEO)
+    a = oracle.runNlBayes(nz, ff, bf, *po, nparts=4, nthreads=2)
+    b = reference.runNlBayes(nz, ff, bf, *pr, nthreads=2)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
