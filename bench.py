@@ -396,16 +396,20 @@ def main():
     forms = {}
     import train_gains
     gains = train_gains.load_weights()
-    variants = [("mixed", {"mixed": True}), ("vbm3d_search", {"vbm3d": True})]
+    variants = [("mixed", {"mixed": True}), ("vbm3d_search", {"vbm3d": True}), ("paste_boost", {})]
     if gains is not None:
         ctx.set_gain_network(gains)
         variants += [("learned", {"learned": True}), ("learned+mixed", {"learned": True, "mixed": True})]
+    import copy
+    q1, q2 = copy.copy(p1), copy.copy(p2)
+    q1.doPasteBoost = q2.doPasteBoost = 1   # the reference's paste trick (nlbParams::doPasteBoost)
     for name, kw in variants:
+        v1, v2 = (q1, q2) if name == "paste_boost" else (p1, p2)
         for _ in range(2):
-            ctx.runNlBayes(d_nz, d_ff, d_bf, p1, p2, basic=d_basic, final=d_final, nparts=args.nparts, **kw)
+            ctx.runNlBayes(d_nz, d_ff, d_bf, v1, v2, basic=d_basic, final=d_final, nparts=args.nparts, **kw)
         tms = []
         for _ in range(args.steps):
-            ctx.runNlBayes(d_nz, d_ff, d_bf, p1, p2, basic=d_basic, final=d_final, nparts=args.nparts, **kw)
+            ctx.runNlBayes(d_nz, d_ff, d_bf, v1, v2, basic=d_basic, final=d_final, nparts=args.nparts, **kw)
             ms, _ = ctx.timings()
             tms.append(ms[4])
         fq = psnr(d_final.cpu().numpy(), clean)

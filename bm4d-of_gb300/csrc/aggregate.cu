@@ -10,6 +10,8 @@
 // and each pixel walks the slots that cover it in that order.  The result is
 // bit-identical to the sequential scatter.
 #include <cuda_runtime.h>
+#include <algorithm>
+#include <vector>
 #include <cstdint>
 
 #include "common.cuh"
@@ -121,6 +123,84 @@ __global__ void kill_apply_kernel(const unsigned long long *__restrict__ edges, 
 			alive[w] = a;
 			*changed = 1u;
 		}
+	}
+}
+
+// Paste trick (doPasteBoost, nldct.cpp:2302-2322 and 2395-2415): a
+// processed group switches off every member's position and its four
+// neighbours outside the border band of 2*sPx, so whether a group is
+// processed depends on all earlier groups of its tile.  One warp per tile
+// walks the tile's groups in processing order, 32 at a time: the batch's
+// switch-off flags and member lists are loaded together, the batch is settled
+// group by group (a processed group's switch-offs inside the batch are OR-ed
+// into the lanes' flags; those of later groups are written to `killed`,
+// which the next batch reads after the warp's own stores).  The grid's
+// inverse maps sit in shared memory.
+__global__ void paste_resolve_kernel(const Tile *__restrict__ tiles, int ntiles, const int *__restrict__ grid,
+                                     StepParams sp, const uint8_t *__restrict__ nsimp,
+                                     const uint32_t *__restrict__ idx, uint8_t *__restrict__ alive,
+                                     uint8_t *killed)
+{
+	extern __shared__ int sm_inv[];
+	const int ti = blockIdx.x;
+	if (ti >= ntiles) return;
+	const Tile T = tiles[ti];
+	const int lane = threadIdx.x;                 // one warp per block
+	int *invx = sm_inv, *invy = invx + T.w, *invf = invy + T.h;
+	uint32_t *mem = reinterpret_cast<uint32_t *>(invf + sp.F);
+	for (int i = lane; i < T.w; i += 32) invx[i] = grid[T.gx + T.nx + i];
+	for (int i = lane; i < T.h; i += 32) invy[i] = grid[T.gy + T.ny + i];
+	for (int i = lane; i < sp.F; i += 32) invf[i] = grid[T.gf + T.nf + i];
+	__syncwarp();
+	const unsigned w = (unsigned)T.w, h = (unsigned)T.h, band = 2u * (unsigned)sp.px;
+	const unsigned F = (unsigned)sp.F;
+	const long long n_t = (long long)T.nx * T.ny * T.nf;
+	for (long long base = 0; base < n_t; base += 32) {
+		const long long g0 = T.g0 + base;
+		const int nb = (int)(n_t - base < 32 ? n_t - base : 32);
+		for (int i = lane; i < nb * sp.np; i += 32) mem[i] = idx[g0 * sp.np + i];
+		int k = lane < nb ? killed[g0 + lane] : 1;
+		const int ns = lane < nb ? nsimp[g0 + lane] : 0;
+		__syncwarp();
+		unsigned done = 0u;
+		for (int j = 0; j < nb; j++) {
+			if (__shfl_sync(0xffffffffu, k, j)) continue;   // switched off earlier
+			done |= 1u << j;
+			const int nsj = __shfl_sync(0xffffffffu, ns, j);
+			const long long gj = g0 + j;
+			unsigned in_batch = 0u;
+			if (lane < nsj) {
+				// member position as the one-channel mask index (t*h + y)*w + x
+				const unsigned ind1 = mem[j * sp.np + lane];
+				const unsigned mx = ind1 % w, my = (ind1 / w) % h, mt = ind1 / (w * h);
+#pragma unroll
+				for (int q = 0; q < 5; q++) {
+					// the position itself, then -w, +w, -1, +1 as linear offsets
+					unsigned vx = mx, vy = my, vt = mt;
+					if (q == 1) { if (!(my > band)) continue; vy = my - 1; }
+					if (q == 2) {
+						if (!(my < h - band)) continue;
+						if (++vy == h) { vy = 0; vt++; }
+					}
+					if (q == 3) { if (!(mx > band)) continue; vx = mx - 1; }
+					if (q == 4) {
+						if (!(mx < w - band)) continue;
+						if (++vx == w) { vx = 0; if (++vy == h) { vy = 0; vt++; } }
+					}
+					if (vt >= F) continue;                      // past the mask
+					const int xi = invx[vx], yi = invy[vy], fi = invf[vt];
+					if (xi < 0 || yi < 0 || fi < 0) continue;   // not a reference position
+					const long long v = T.g0 + ((long long)fi * T.ny + yi) * T.nx + xi;
+					if (v <= gj) continue;                      // already settled
+					if (v < g0 + nb) in_batch |= 1u << (unsigned)(v - g0);
+					else killed[v] = 1;
+				}
+			}
+			in_batch = __reduce_or_sync(0xffffffffu, in_batch);
+			if ((in_batch >> lane) & 1u) k = 1;
+		}
+		if (lane < nb) alive[g0 + lane] = (uint8_t)((done >> lane) & 1u);
+		__syncwarp();
 	}
 }
 
@@ -526,6 +606,24 @@ cudaError_t launch_kill_fixpoint(const unsigned long long *edges, const unsigned
                                  uint8_t *alive, uint8_t *killed, cudaStream_t st)
 {
 	kill_fixpoint_kernel<<<1, 1024, 0, st>>>(edges, nedges, cap, alive, killed);
+	return cudaGetLastError();
+}
+
+size_t paste_smem_bytes(const std::vector<Tile> &tiles, const StepParams &sp)
+{
+	int most = 0;
+	for (const Tile &T : tiles) most = std::max(most, T.w + T.h);
+	return sizeof(int) * ((size_t)most + sp.F + 32 * (size_t)sp.np);
+}
+
+cudaError_t launch_paste_resolve(const Tile *tiles, int ntiles, const int *grid, const StepParams &sp,
+                                 const uint8_t *nsimp, const uint32_t *idx, uint8_t *alive, uint8_t *killed,
+                                 size_t smem, cudaStream_t st)
+{
+	cudaError_t e = cudaFuncSetAttribute(paste_resolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                     (int)smem);
+	if (e != cudaSuccess) return e;
+	paste_resolve_kernel<<<ntiles, 32, smem, st>>>(tiles, ntiles, grid, sp, nsimp, idx, alive, killed);
 	return cudaGetLastError();
 }
 

@@ -55,6 +55,7 @@ struct StepParams {               // resolved parameters of one step
 	int vbm3d;                    // predictive search (the reference's VBM3D_SEARCH build)
 	int wxp, npf;                 // sizeSearchWindowPred, nSimilarPatchesPred
 	float dsub_bias;              // dsub*dsub*255 (nldct.cpp:921)
+	int paste;                    // doPasteBoost
 };
 
 // Locate the tile owning global group g (tiles are few: linear scan).

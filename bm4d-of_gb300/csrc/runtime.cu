@@ -256,7 +256,6 @@ bm4dof_status check_params(const bm4dof_params &p)
 	else if (spc > (unsigned)kMaxSpc) why = "sizePatch^2 * sizePatchTime must be at most 64";
 	else if (p.sizeSearchWindow == 0) why = "sizeSearchWindow must be positive";
 	else if (p.sizeSearchTimeRangeFwd + p.sizeSearchTimeRangeBwd + 1 > (unsigned)kMaxFrames) why = "temporal search range too long";
-	else if (p.doPasteBoost) why = "doPasteBoost is not supported";
 	else if (p.sigma <= 0.f) why = "sigma must be positive";
 	if (!why.empty()) {
 		set_error("bm4dof: unsupported parameters: " + why);
@@ -300,6 +299,7 @@ struct StepState {
 	long long G = 0, chunk = 0;
 	bool mixed_search = false;
 	size_t nblocks = 0;
+	size_t paste_smem = 0;                // doPasteBoost: shared memory of the settling kernel
 	Tile *d_tiles = nullptr;
 	int *d_grid = nullptr;
 	float *d_basis = nullptr, *d_binv = nullptr, *d_win = nullptr;
@@ -416,6 +416,12 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	sp.wxp = (int)p.sizeSearchWindowPred;
 	sp.npf = (int)p.nSimilarPatchesPred;
 	sp.dsub_bias = p.dsub * p.dsub * 255.f;   // nldct.cpp:921, float
+	sp.paste = p.doPasteBoost ? 1 : 0;
+	S.paste_smem = sp.paste ? paste_smem_bytes(pl.tiles, sp) : 0;
+	if (S.paste_smem > (size_t)200 * 1024) {
+		set_error("bm4dof: doPasteBoost: tiles too large");
+		return BM4DOF_ERR_UNSUPPORTED;
+	}
 	if (sp.vbm3d) {
 		std::string why;
 		if (!vbm3d_check(sp, pl.tiles, why)) {
@@ -568,7 +574,16 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 	}
 
 	// ---- mask switch-offs (rare): killer -> victim edges, then fixed point --
-	{
+	// (doPasteBoost: every processed group switches off its members' positions
+	// and their neighbours, settled tile by tile in processing order)
+	if (sp.paste) {
+		Mark m(ctx, T_OTHER);
+		CK(cudaMemsetAsync(S.d_killed, 0, G, st));
+		CK(launch_paste_resolve(S.d_tiles, ntiles, S.d_grid, sp, S.d_nsimp, S.d_idx, S.d_alive, S.d_killed,
+		                        S.paste_smem, st));
+		CK(launch_count_alive(S.d_tiles, ntiles, G, S.d_alive, S.d_small + 64, st));
+		ctx->launches += 2;
+	} else {
 		Mark m(ctx, T_OTHER);
 		CK(cudaMemsetAsync(S.d_alive, 1, G, st));
 		CK(launch_kill_edges(S.d_tiles, ntiles, S.d_grid, S.d_grid, sp, G, S.d_idx, S.d_edges, S.d_small,

@@ -972,11 +972,15 @@ unsigned process_tile(const Vid &noisy, const Vid &fflow, const Vid &bflow, Vid 
 						const unsigned ind = index[n];
 						const unsigned ind1 = (ind / whc) * wh + ind % wh;
 						const unsigned mx = ind1 % W, my = (ind1 / W) % H;
+						/* linear neighbours, as the reference writes them (a band
+						 * wider than the tile lets +1 / +W cross into the next row
+						 * or frame); writes past the mask are skipped */
+						const size_t msz = mask.size();
 						mask[ind1] = 0;
 						if (my > 2 * sPx) mask[ind1 - W] = 0;
-						if (my < H - 2 * sPx) mask[ind1 + W] = 0;
+						if (my < H - 2 * sPx && ind1 + W < msz) mask[ind1 + W] = 0;
 						if (mx > 2 * sPx) mask[ind1 - 1] = 0;
-						if (mx < W - 2 * sPx) mask[ind1 + 1] = 0;
+						if (mx < W - 2 * sPx && ind1 + 1 < msz) mask[ind1 + 1] = 0;
 					}
 				} else {
 					/* mask(index[0]) = false, nldct.cpp:2325-2329: the index carries
