@@ -10,11 +10,10 @@
 // and each pixel walks the slots that cover it in that order.  The result is
 // bit-identical to the sequential scatter.
 #include <cuda_runtime.h>
-#include <algorithm>
-#include <vector>
 #include <cstdint>
 
 #include "common.cuh"
+#include "internal.hpp"
 
 namespace bm4dof {
 
@@ -128,80 +127,136 @@ __global__ void kill_apply_kernel(const unsigned long long *__restrict__ edges, 
 
 // Paste trick (doPasteBoost, nldct.cpp:2302-2322 and 2395-2415): a
 // processed group switches off every member's position and its four
-// neighbours outside the border band of 2*sPx, so whether a group is
-// processed depends on all earlier groups of its tile.  One warp per tile
-// walks the tile's groups in processing order, 32 at a time: the batch's
-// switch-off flags and member lists are loaded together, the batch is settled
-// group by group (a processed group's switch-offs inside the batch are OR-ed
-// into the lanes' flags; those of later groups are written to `killed`,
-// which the next batch reads after the warp's own stores).  The grid's
-// inverse maps sit in shared memory.
-__global__ void paste_resolve_kernel(const Tile *__restrict__ tiles, int ntiles, const int *__restrict__ grid,
-                                     StepParams sp, const uint8_t *__restrict__ nsimp,
-                                     const uint32_t *__restrict__ idx, uint8_t *__restrict__ alive,
-                                     uint8_t *killed)
+// neighbours outside the border band of 2*sPx (linear offsets -w, +w, -1, +1,
+// so a band wider than the tile crosses rows; unsigned comparisons as the
+// reference's).  Only reference positions are ever read from the mask, so a
+// switch-off is an edge from a group to a later group of its tile, and a
+// group is processed exactly when none of its killers is:
+//     alive(g) = no alive k < g with an edge k -> g,
+// the reference's sequential order restated as a recursion with one solution.
+// It is evaluated by frontier rounds: a group is settled dead as soon as one
+// killer is alive, alive once all its killers are dead (a count of pending
+// killers per group); each settled group is pushed once and, when popped,
+// settles or counts down its victims.  The first rounds run over the whole
+// GPU, the tail in one CTA; every round count is fixed on the host side, so
+// the sequence is stream ordered and graph capturable.
+constexpr unsigned kUndecided = 0u, kAlive = 1u, kDead = 2u;
+
+template <class Fn>
+__device__ __forceinline__ void paste_victims(const Tile &T, const int *__restrict__ grid, const StepParams &sp,
+                                              long long g, const uint8_t *__restrict__ nsimp,
+                                              const uint32_t *__restrict__ idx, Fn fn)
 {
-	extern __shared__ int sm_inv[];
-	const int ti = blockIdx.x;
-	if (ti >= ntiles) return;
-	const Tile T = tiles[ti];
-	const int lane = threadIdx.x;                 // one warp per block
-	int *invx = sm_inv, *invy = invx + T.w, *invf = invy + T.h;
-	uint32_t *mem = reinterpret_cast<uint32_t *>(invf + sp.F);
-	for (int i = lane; i < T.w; i += 32) invx[i] = grid[T.gx + T.nx + i];
-	for (int i = lane; i < T.h; i += 32) invy[i] = grid[T.gy + T.ny + i];
-	for (int i = lane; i < sp.F; i += 32) invf[i] = grid[T.gf + T.nf + i];
-	__syncwarp();
-	const unsigned w = (unsigned)T.w, h = (unsigned)T.h, band = 2u * (unsigned)sp.px;
-	const unsigned F = (unsigned)sp.F;
-	const long long n_t = (long long)T.nx * T.ny * T.nf;
-	for (long long base = 0; base < n_t; base += 32) {
-		const long long g0 = T.g0 + base;
-		const int nb = (int)(n_t - base < 32 ? n_t - base : 32);
-		for (int i = lane; i < nb * sp.np; i += 32) mem[i] = idx[g0 * sp.np + i];
-		int k = lane < nb ? killed[g0 + lane] : 1;
-		const int ns = lane < nb ? nsimp[g0 + lane] : 0;
-		__syncwarp();
-		unsigned done = 0u;
-		for (int j = 0; j < nb; j++) {
-			if (__shfl_sync(0xffffffffu, k, j)) continue;   // switched off earlier
-			done |= 1u << j;
-			const int nsj = __shfl_sync(0xffffffffu, ns, j);
-			const long long gj = g0 + j;
-			unsigned in_batch = 0u;
-			if (lane < nsj) {
-				// member position as the one-channel mask index (t*h + y)*w + x
-				const unsigned ind1 = mem[j * sp.np + lane];
-				const unsigned mx = ind1 % w, my = (ind1 / w) % h, mt = ind1 / (w * h);
+	const unsigned w = (unsigned)T.w, h = (unsigned)T.h, band = 2u * (unsigned)sp.px, F = (unsigned)sp.F;
+	const int ns = nsimp[g];
+	for (int m = 0; m < ns; m++) {
+		// member position as the one-channel mask index (t*h + y)*w + x
+		const unsigned ind1 = idx[g * sp.np + m];
+		const unsigned mx = ind1 % w, my = (ind1 / w) % h, mt = ind1 / (w * h);
 #pragma unroll
-				for (int q = 0; q < 5; q++) {
-					// the position itself, then -w, +w, -1, +1 as linear offsets
-					unsigned vx = mx, vy = my, vt = mt;
-					if (q == 1) { if (!(my > band)) continue; vy = my - 1; }
-					if (q == 2) {
-						if (!(my < h - band)) continue;
-						if (++vy == h) { vy = 0; vt++; }
-					}
-					if (q == 3) { if (!(mx > band)) continue; vx = mx - 1; }
-					if (q == 4) {
-						if (!(mx < w - band)) continue;
-						if (++vx == w) { vx = 0; if (++vy == h) { vy = 0; vt++; } }
-					}
-					if (vt >= F) continue;                      // past the mask
-					const int xi = invx[vx], yi = invy[vy], fi = invf[vt];
-					if (xi < 0 || yi < 0 || fi < 0) continue;   // not a reference position
-					const long long v = T.g0 + ((long long)fi * T.ny + yi) * T.nx + xi;
-					if (v <= gj) continue;                      // already settled
-					if (v < g0 + nb) in_batch |= 1u << (unsigned)(v - g0);
-					else killed[v] = 1;
-				}
+		for (int q = 0; q < 5; q++) {
+			unsigned vx = mx, vy = my, vt = mt;
+			if (q == 1) { if (!(my > band)) continue; vy = my - 1; }
+			if (q == 2) {
+				if (!(my < h - band)) continue;
+				if (++vy == h) { vy = 0; vt++; }
 			}
-			in_batch = __reduce_or_sync(0xffffffffu, in_batch);
-			if ((in_batch >> lane) & 1u) k = 1;
+			if (q == 3) { if (!(mx > band)) continue; vx = mx - 1; }
+			if (q == 4) {
+				if (!(mx < w - band)) continue;
+				if (++vx == w) { vx = 0; if (++vy == h) { vy = 0; vt++; } }
+			}
+			if (vt >= F) continue;                          // past the mask
+			const int xi = grid[T.gx + T.nx + vx], yi = grid[T.gy + T.ny + vy], fi = grid[T.gf + T.nf + vt];
+			if (xi < 0 || yi < 0 || fi < 0) continue;       // not a reference position
+			const long long v = T.g0 + ((long long)fi * T.ny + yi) * T.nx + xi;
+			if (v > g) fn(v);                               // earlier groups are settled already
 		}
-		if (lane < nb) alive[g0 + lane] = (uint8_t)((done >> lane) & 1u);
-		__syncwarp();
 	}
+}
+
+__global__ void paste_count_kernel(const Tile *__restrict__ tiles, int ntiles, const int *__restrict__ grid,
+                                   StepParams sp, long long G, const uint8_t *__restrict__ nsimp,
+                                   const uint32_t *__restrict__ idx, unsigned *__restrict__ pending)
+{
+	for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < G;
+	     g += (long long)gridDim.x * blockDim.x) {
+		const Tile T = tiles[tile_of(tiles, ntiles, g)];
+		paste_victims(T, grid, sp, g, nsimp, idx, [&](long long v) { atomicAdd(&pending[v], 1u); });
+	}
+}
+
+__global__ void paste_init_kernel(long long G, const unsigned *__restrict__ pending, unsigned *__restrict__ state,
+                                  uint32_t *__restrict__ queue, unsigned *__restrict__ count)
+{
+	for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < G;
+	     g += (long long)gridDim.x * blockDim.x) {
+		const bool free_ = pending[g] == 0u;
+		state[g] = free_ ? kAlive : kUndecided;
+		if (free_) queue[atomicAdd(count, 1u)] = (uint32_t)g;
+	}
+}
+
+// Pops group g: an alive group settles its undecided victims dead, a dead
+// one counts them down (the last killer to die settles a victim alive).
+__device__ __forceinline__ void paste_settle(const Tile *__restrict__ tiles, int ntiles,
+                                             const int *__restrict__ grid, const StepParams &sp, long long g,
+                                             const uint8_t *__restrict__ nsimp, const uint32_t *__restrict__ idx,
+                                             unsigned *state, unsigned *pending, uint32_t *qout, unsigned *nout)
+{
+	const Tile T = tiles[tile_of(tiles, ntiles, g)];
+	const unsigned sg = state[g];
+	paste_victims(T, grid, sp, g, nsimp, idx, [&](long long v) {
+		if (sg == kAlive) {
+			if (atomicCAS(&state[v], kUndecided, kDead) == kUndecided) qout[atomicAdd(nout, 1u)] = (uint32_t)v;
+		} else if (atomicSub(&pending[v], 1u) == 1u) {
+			if (atomicCAS(&state[v], kUndecided, kAlive) == kUndecided) qout[atomicAdd(nout, 1u)] = (uint32_t)v;
+		}
+	});
+}
+
+__global__ void paste_round_kernel(const Tile *__restrict__ tiles, int ntiles, const int *__restrict__ grid,
+                                   StepParams sp, const uint8_t *__restrict__ nsimp,
+                                   const uint32_t *__restrict__ idx, unsigned *state, unsigned *pending,
+                                   const uint32_t *__restrict__ qin, const unsigned *__restrict__ nin,
+                                   uint32_t *__restrict__ qout, unsigned *nout)
+{
+	const unsigned n = *nin;
+	for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		paste_settle(tiles, ntiles, grid, sp, qin[i], nsimp, idx, state, pending, qout, nout);
+}
+
+// The remaining rounds in one CTA (small frontiers), until the frontier is
+// empty: every group is pushed at most once, so at most G + 1 rounds.
+__global__ void __launch_bounds__(1024)
+paste_finish_kernel(const Tile *__restrict__ tiles, int ntiles, const int *__restrict__ grid, StepParams sp,
+                    long long G, const uint8_t *__restrict__ nsimp, const uint32_t *__restrict__ idx,
+                    unsigned *state, unsigned *pending, uint32_t *q0, uint32_t *q1, unsigned *n_in,
+                    unsigned *n_pair)
+{
+	uint32_t *qin = q0, *qout = q1;
+	unsigned *nin = n_in;
+	for (long long r = 0; r <= G; r++) {
+		unsigned *nout = n_pair + (r & 1);
+		if (threadIdx.x == 0) *nout = 0u;
+		__syncthreads();
+		const unsigned n = *(volatile unsigned *)nin;
+		if (n == 0u) break;
+		for (unsigned i = threadIdx.x; i < n; i += blockDim.x)
+			paste_settle(tiles, ntiles, grid, sp, qin[i], nsimp, idx, state, pending, qout, nout);
+		__syncthreads();
+		uint32_t *t = qin;
+		qin = qout;
+		qout = t;
+		nin = nout;
+	}
+}
+
+__global__ void paste_alive_kernel(long long G, const unsigned *__restrict__ state, uint8_t *__restrict__ alive)
+{
+	for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < G;
+	     g += (long long)gridDim.x * blockDim.x)
+		alive[g] = state[g] == kAlive ? 1 : 0;
 }
 
 __global__ void count_alive_kernel(const Tile *__restrict__ tiles, int ntiles, long long G,
@@ -609,21 +664,27 @@ cudaError_t launch_kill_fixpoint(const unsigned long long *edges, const unsigned
 	return cudaGetLastError();
 }
 
-size_t paste_smem_bytes(const std::vector<Tile> &tiles, const StepParams &sp)
+cudaError_t launch_paste_resolve(const Tile *tiles, int ntiles, const int *grid, const StepParams &sp, long long G,
+                                 const uint8_t *nsimp, const uint32_t *idx, PasteScratch w, uint8_t *alive, int nsm,
+                                 cudaStream_t st)
 {
-	int most = 0;
-	for (const Tile &T : tiles) most = std::max(most, T.w + T.h);
-	return sizeof(int) * ((size_t)most + sp.F + 32 * (size_t)sp.np);
-}
-
-cudaError_t launch_paste_resolve(const Tile *tiles, int ntiles, const int *grid, const StepParams &sp,
-                                 const uint8_t *nsimp, const uint32_t *idx, uint8_t *alive, uint8_t *killed,
-                                 size_t smem, cudaStream_t st)
-{
-	cudaError_t e = cudaFuncSetAttribute(paste_resolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                                     (int)smem);
+	if (G <= 0) return cudaSuccess;
+	cudaError_t e = cudaMemsetAsync(w.pending, 0, sizeof(unsigned) * (size_t)G, st);
+	if (e == cudaSuccess) e = cudaMemsetAsync(w.counts, 0, sizeof(unsigned) * (kPasteRounds + 3), st);
 	if (e != cudaSuccess) return e;
-	paste_resolve_kernel<<<ntiles, 32, smem, st>>>(tiles, ntiles, grid, sp, nsimp, idx, alive, killed);
+	const int b = grid_for(G, 256, 8 * nsm);
+	paste_count_kernel<<<b, 256, 0, st>>>(tiles, ntiles, grid, sp, G, nsimp, idx, w.pending);
+	paste_init_kernel<<<b, 256, 0, st>>>(G, w.pending, w.state, w.q0, w.counts);
+	// the wide rounds: round r reads counts[r] and queue r & 1
+	for (int r = 0; r < kPasteRounds; r++)
+		paste_round_kernel<<<b, 256, 0, st>>>(tiles, ntiles, grid, sp, nsimp, idx, w.state, w.pending,
+		                                      (r & 1) ? w.q1 : w.q0, w.counts + r, (r & 1) ? w.q0 : w.q1,
+		                                      w.counts + r + 1);
+	const bool odd = (kPasteRounds & 1) != 0;
+	paste_finish_kernel<<<1, 1024, 0, st>>>(tiles, ntiles, grid, sp, G, nsimp, idx, w.state, w.pending,
+	                                        odd ? w.q1 : w.q0, odd ? w.q0 : w.q1, w.counts + kPasteRounds,
+	                                        w.counts + kPasteRounds + 1);
+	paste_alive_kernel<<<b, 256, 0, st>>>(G, w.state, alive);
 	return cudaGetLastError();
 }
 

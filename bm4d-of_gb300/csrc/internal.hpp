@@ -64,11 +64,17 @@ cudaError_t launch_kill_iteration(const unsigned long long *edges, unsigned n, u
 // Switch-offs resolved on the device in one launch (no host round trip).
 cudaError_t launch_kill_fixpoint(const unsigned long long *edges, const unsigned *nedges, unsigned cap,
                                  uint8_t *alive, uint8_t *killed, cudaStream_t st);
-// Paste trick (doPasteBoost): processed groups settled tile by tile.
-size_t paste_smem_bytes(const std::vector<Tile> &tiles, const StepParams &sp);
-cudaError_t launch_paste_resolve(const Tile *tiles, int ntiles, const int *grid, const StepParams &sp,
-                                 const uint8_t *nsimp, const uint32_t *idx, uint8_t *alive, uint8_t *killed,
-                                 size_t smem, cudaStream_t st);
+// Paste trick (doPasteBoost): the processed groups, settled by frontier
+// rounds (kPasteRounds over the whole GPU, the rest in one CTA).
+constexpr int kPasteRounds = 24;
+struct PasteScratch {
+	unsigned *pending, *state;   // G each
+	uint32_t *q0, *q1;           // G each
+	unsigned *counts;            // kPasteRounds + 3
+};
+cudaError_t launch_paste_resolve(const Tile *tiles, int ntiles, const int *grid, const StepParams &sp, long long G,
+                                 const uint8_t *nsimp, const uint32_t *idx, PasteScratch w, uint8_t *alive, int nsm,
+                                 cudaStream_t st);
 cudaError_t launch_count_alive(const Tile *tiles, int ntiles, long long G, const uint8_t *alive,
                                unsigned *counts, cudaStream_t st);
 cudaError_t exclusive_scan(unsigned *data, size_t n, unsigned *scratch, cudaStream_t st);

@@ -299,7 +299,7 @@ struct StepState {
 	long long G = 0, chunk = 0;
 	bool mixed_search = false;
 	size_t nblocks = 0;
-	size_t paste_smem = 0;                // doPasteBoost: shared memory of the settling kernel
+	PasteScratch paste = {nullptr, nullptr, nullptr, nullptr, nullptr};   // doPasteBoost only
 	Tile *d_tiles = nullptr;
 	int *d_grid = nullptr;
 	float *d_basis = nullptr, *d_binv = nullptr, *d_win = nullptr;
@@ -417,11 +417,6 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	sp.npf = (int)p.nSimilarPatchesPred;
 	sp.dsub_bias = p.dsub * p.dsub * 255.f;   // nldct.cpp:921, float
 	sp.paste = p.doPasteBoost ? 1 : 0;
-	S.paste_smem = sp.paste ? paste_smem_bytes(pl.tiles, sp) : 0;
-	if (S.paste_smem > (size_t)200 * 1024) {
-		set_error("bm4dof: doPasteBoost: tiles too large");
-		return BM4DOF_ERR_UNSUPPORTED;
-	}
 	if (sp.vbm3d) {
 		std::string why;
 		if (!vbm3d_check(sp, pl.tiles, why)) {
@@ -487,6 +482,13 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	SBUF("traj", (size_t)G * search_frames_max(sp), S.d_traj);
 	SBUF("edges", G, S.d_edges);   // a group switches off at most one other
 	if (S.mixed_search) SBUF("mixed_blocks", blocks.size(), S.d_blocks);
+	if (sp.paste) {
+		SBUF("paste_pending", G, S.paste.pending);
+		SBUF("paste_state", G, S.paste.state);
+		SBUF("paste_q0", G, S.paste.q0);
+		SBUF("paste_q1", G, S.paste.q1);
+		SBUF("paste_counts", kPasteRounds + 3, S.paste.counts);
+	}
 
 	// shared aggregation buffers; chunks of groups whose slot terms (vals),
 	// weights, origin lists and spatial lists fit the slot budget; slot
@@ -578,11 +580,10 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 	// and their neighbours, settled tile by tile in processing order)
 	if (sp.paste) {
 		Mark m(ctx, T_OTHER);
-		CK(cudaMemsetAsync(S.d_killed, 0, G, st));
-		CK(launch_paste_resolve(S.d_tiles, ntiles, S.d_grid, sp, S.d_nsimp, S.d_idx, S.d_alive, S.d_killed,
-		                        S.paste_smem, st));
+		CK(launch_paste_resolve(S.d_tiles, ntiles, S.d_grid, sp, G, S.d_nsimp, S.d_idx, S.paste, S.d_alive,
+		                        ctx->nsm, st));
 		CK(launch_count_alive(S.d_tiles, ntiles, G, S.d_alive, S.d_small + 64, st));
-		ctx->launches += 2;
+		ctx->launches += kPasteRounds + 5;
 	} else {
 		Mark m(ctx, T_OTHER);
 		CK(cudaMemsetAsync(S.d_alive, 1, G, st));
