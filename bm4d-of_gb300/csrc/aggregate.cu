@@ -461,12 +461,13 @@ __global__ void slist_build_kernel(int w, int h, int F, int px_rt, int pt, int t
 // reference's scatter loop adds them.  PT > 0 keeps the pt list heads in
 // registers; CC is the channel count.  Each list's next entry is fetched one
 // step ahead, so that the load of the term being added and the list advance
-// overlap instead of forming one dependent chain per term.
+// overlap instead of forming one dependent chain per term.  A term's C
+// estimates and its weight term w * window[p] sit side by side in `vals`
+// (term_stride), so each term is one vector load from one 32-byte sector.
 template <int PT, int CC>
 __global__ void __launch_bounds__(128)
 gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *__restrict__ soff,
-                    const unsigned *__restrict__ sl, const float *__restrict__ vals,
-                    const float *__restrict__ wslot, const float *__restrict__ win, float *__restrict__ acc,
+                    const unsigned *__restrict__ sl, const float *__restrict__ vals, float *__restrict__ acc,
                     float *__restrict__ wacc)
 {
 	constexpr int L = PT > 0 ? PT : kMaxSpc;
@@ -510,11 +511,24 @@ gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *_
 			const unsigned slot = best >> 6;
 			const int dx = best & 7, dy = (best >> 3) & 7;
 			const int p = (bl * px + dy) * px + dx;
-			const float *v = vals + (size_t)slot * (CC * spc) + p;
-			float x[CC];
+			// the C estimates and the weight term of (slot, p): one vector load
+			constexpr int TS = CC == 1 ? 2 : (CC <= 3 ? 4 : 8);
+			const float *v = vals + ((size_t)slot * spc + p) * TS;
+			float x[TS];
+			if (TS == 2) {
+				const float2 q = __ldg(reinterpret_cast<const float2 *>(v));
+				x[0] = q.x;
+				x[1] = q.y;
+			} else {
 #pragma unroll
-			for (int c = 0; c < CC; c++) x[c] = __ldg(v + c * spc);
-			const float ws = __ldg(wslot + slot);
+				for (int h = 0; h < TS / 4; h++) {
+					const float4 q = __ldg(reinterpret_cast<const float4 *>(v) + h);
+					x[4 * h] = q.x;
+					x[4 * h + 1] = q.y;
+					x[4 * h + 2] = q.z;
+					x[4 * h + 3] = q.w;
+				}
+			}
 #pragma unroll
 			for (int l = 0; l < L; l++)
 				if (l == bl) {
@@ -524,7 +538,7 @@ gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *_
 				}
 #pragma unroll
 			for (int c = 0; c < CC; c++) a[c] = __fadd_rn(a[c], x[c]);
-			wa = __fadd_rn(wa, __fmul_rn(ws, win[p]));
+			wa = __fadd_rn(wa, x[CC]);   // w * window[p], as the reference forms it
 		}
 		wacc[pix] = wa;
 #pragma unroll
@@ -534,14 +548,13 @@ gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *_
 
 template <int CC>
 void gather_pt(int gb, cudaStream_t st, const Tile &T, const StepParams &sp, int t_lo, int f_hi,
-               const unsigned *soff, const unsigned *sl, const float *vals, const float *wslot, const float *win,
-               float *acc, float *wacc)
+               const unsigned *soff, const unsigned *sl, const float *vals, float *acc, float *wacc)
 {
 	switch (sp.pt) {
-	case 1: gather_slist_kernel<1, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
-	case 2: gather_slist_kernel<2, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
-	case 4: gather_slist_kernel<4, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
-	default: gather_slist_kernel<0, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc); break;
+	case 1: gather_slist_kernel<1, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, acc, wacc); break;
+	case 2: gather_slist_kernel<2, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, acc, wacc); break;
+	case 4: gather_slist_kernel<4, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, acc, wacc); break;
+	default: gather_slist_kernel<0, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, f_hi, soff, sl, vals, acc, wacc); break;
 	}
 }
 
@@ -728,8 +741,7 @@ cudaError_t launch_lists(long long ga, long long gb, int np, const uint8_t *nsim
 
 cudaError_t launch_gather(const Tile &T, const StepParams &sp, int t_lo, int t_hi, const unsigned *off,
                           const unsigned *list, unsigned *soff, unsigned *sl, unsigned *scratch,
-                          const float *vals, const float *wslot, const float *win, float *acc, float *wacc,
-                          cudaStream_t st)
+                          const float *vals, float *acc, float *wacc, cudaStream_t st)
 {
 	// origin frames [t_lo, t_hi] hold the chunk's member patches; pixels of
 	// frames [t_lo, t_hi + pt - 1] receive them
@@ -746,9 +758,9 @@ cudaError_t launch_gather(const Tile &T, const StepParams &sp, int t_lo, int t_h
 	const int f_hi = t_hi + sp.pt - 1 < sp.F - 1 ? t_hi + sp.pt - 1 : sp.F - 1;
 	const long long npix = (long long)T.w * T.h * (f_hi - t_lo + 1);
 	const int gb = grid_for(npix, 128, 65535);
-	if (sp.C == 1) gather_pt<1>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc);
-	else if (sp.C == 3) gather_pt<3>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc);
-	else gather_pt<4>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, wslot, win, acc, wacc);
+	if (sp.C == 1) gather_pt<1>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, acc, wacc);
+	else if (sp.C == 3) gather_pt<3>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, acc, wacc);
+	else gather_pt<4>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, acc, wacc);
 	return cudaGetLastError();
 }
 

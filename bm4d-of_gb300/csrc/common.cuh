@@ -58,6 +58,13 @@ struct StepParams {               // resolved parameters of one step
 	int paste;                    // doPasteBoost
 };
 
+// Aggregation terms of a chunk of groups: for slot s (one member of one
+// group) and patch element p, the C weighted estimates (w * window[p]) * ghat
+// followed by the weight term w * window[p], so that the ordered gather reads
+// one aligned vector per term:  vals[(s * spc + p) * term_stride(C) + c],
+// c = 0..C (c = C: the weight term).
+__host__ __device__ __forceinline__ int term_stride(int C) { return C == 1 ? 2 : (C <= 3 ? 4 : 8); }
+
 // Locate the tile owning global group g (tiles are few: linear scan).
 __device__ __forceinline__ int tile_of(const Tile *tiles, int ntiles, long long g)
 {

@@ -245,10 +245,13 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
 				for (int n = 1; n < ns; n++) differs |= row[n] != row[0];
 			}
 		const int any = __syncthreads_or(differs);
+		const int ts = term_stride(C);
 		if (ns > 1 && !any) {
+			// unweighted: the weights are set later (fixup_equal_kernel)
 			for (int it = tid; it < ns * per; it += blockDim.x) {
 				const int n = it / per, r = it % per;
-				vals[(slot0 + n) * per + r] = Gn[r * nsp + n];
+				const int c = r / spc, p = r % spc;
+				vals[((slot0 + n) * spc + p) * ts + c] = Gn[r * nsp + n];
 			}
 			if (tid == 0) eq[g] = 1;
 			continue;
@@ -311,8 +314,12 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
 		const float w = s_w;
 		for (int it = tid; it < ns * per; it += blockDim.x) {
 			const int n = it / per, r = it % per;
-			const int p = r % spc;
-			vals[(slot0 + n) * per + r] = __fmul_rn(__fmul_rn(w, wn[p]), Gn[r * nsp + n]);
+			const int c = r / spc, p = r % spc;
+			vals[((slot0 + n) * spc + p) * ts + c] = __fmul_rn(__fmul_rn(w, wn[p]), Gn[r * nsp + n]);
+		}
+		for (int it = tid; it < ns * spc; it += blockDim.x) {
+			const int n = it / spc, p = it % spc;
+			vals[((slot0 + n) * spc + p) * ts + C] = __fmul_rn(w, wn[p]);
 		}
 		if (tid < ns) wslot[slot0 + tid] = w;
 		if (tid == 0) { wgroup[g] = w; eq[g] = 0; }
@@ -430,7 +437,8 @@ filter_quad_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, int
 		if (lane == 0) s_flag[sub][w] = differs;
 		quad_sync(bar);
 		if (ns > 1 && !(s_flag[sub][0] | s_flag[sub][1])) {
-			for (int n = 0; n < ns; n++) vals[(slot0 + n) * SPC + t] = Gn[t * nsp + n];
+			for (int n = 0; n < ns; n++)
+				reinterpret_cast<float2 *>(vals)[(slot0 + n) * SPC + t] = make_float2(Gn[t * nsp + n], 0.f);
 			if (t == 0) eq[g] = 1;
 			quad_sync(bar);
 			continue;
@@ -471,7 +479,8 @@ filter_quad_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, int
 		quad_sync(bar);
 		const float wg = s_w[sub];
 		const float wp = __fmul_rn(wg, wn[t]);
-		for (int n = 0; n < ns; n++) vals[(slot0 + n) * SPC + t] = __fmul_rn(wp, Gn[t * nsp + n]);
+		for (int n = 0; n < ns; n++)
+			reinterpret_cast<float2 *>(vals)[(slot0 + n) * SPC + t] = make_float2(__fmul_rn(wp, Gn[t * nsp + n]), wp);
 		if (t < ns) wslot[slot0 + t] = wg;
 		if (t == 0) { wgroup[g] = wg; eq[g] = 0; }
 		quad_sync(bar);
@@ -501,8 +510,13 @@ __global__ void fixup_equal_kernel(const Tile *__restrict__ tiles, int ntiles, S
 			for (long long q = g - 1; q >= T.g0; q--)
 				if (alive[q] && !eq[q] && nsimp[q] > n) { w = wgroup[q]; break; }
 			wslot[slot0 + n] = w;
-			float *v = vals + (slot0 + n) * per;
-			for (int r = 0; r < per; r++) v[r] = __fmul_rn(__fmul_rn(w, win[r % sp.spc]), v[r]);
+			const int ts = term_stride(sp.C);
+			float *v = vals + (slot0 + n) * sp.spc * ts;
+			for (int p = 0; p < sp.spc; p++) {
+				const float wp = __fmul_rn(w, win[p]);
+				for (int c = 0; c < sp.C; c++) v[p * ts + c] = __fmul_rn(wp, v[p * ts + c]);
+				v[p * ts + sp.C] = wp;
+			}
 		}
 	}
 }

@@ -86,8 +86,7 @@ cudaError_t launch_lists(long long ga, long long gb, int np, const uint8_t *nsim
 // per-pixel merge over origin frames.
 cudaError_t launch_gather(const Tile &T, const StepParams &sp, int t_lo, int t_hi,
                           const unsigned *off, const unsigned *list, unsigned *soff, unsigned *sl,
-                          unsigned *scratch, const float *vals, const float *wslot, const float *win,
-                          float *acc, float *wacc, cudaStream_t st);
+                          unsigned *scratch, const float *vals, float *acc, float *wacc, cudaStream_t st);
 cudaError_t launch_color(const Image &in, const Image &out, int forward, cudaStream_t st);
 cudaError_t launch_finalize(const Tile *tiles, int nW, int wTmp, int hTmp, const StepParams &sp,
                             const Image &noisy, const float *acc, const float *wacc,

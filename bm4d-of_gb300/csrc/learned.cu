@@ -235,7 +235,8 @@ __device__ void group_body(const LearnedArgs &a, const StepParams &sp, long long
 	const long long slot0 = r * sp.np;
 	const float wp = wgt * win[k];
 #pragma unroll
-	for (int m = 0; m < NS; m++) a.vals[(slot0 + m) * kSpc + k] = wp * est[m];
+	for (int m = 0; m < NS; m++)
+		reinterpret_cast<float2 *>(a.vals)[(slot0 + m) * kSpc + k] = make_float2(wp * est[m], wp);
 	if (k < NS) a.wslot[slot0 + k] = wgt;
 }
 
@@ -460,7 +461,8 @@ __device__ void tc_group(const LearnedArgs &a, const StepParams &sp, long long g
 		const int p = lane + 32 * h;
 		const float wp = wgt * win[p];
 #pragma unroll
-		for (int m = 0; m < NS; m++) a.vals[(slot0 + m) * kSpc + p] = wp * W.Z[p][m];
+		for (int m = 0; m < NS; m++)
+			reinterpret_cast<float2 *>(a.vals)[(slot0 + m) * kSpc + p] = make_float2(wp * W.Z[p][m], wp);
 	}
 	if (lane < NS) a.wslot[slot0 + lane] = wgt;
 }

@@ -499,7 +499,7 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	DBUF("off", pl.maxpos + 1, S.d_off);
 	DBUF("soff", pl.maxpos + 1, S.d_soff);
 	DBUF("scratch", pl.maxpos / 4096 + pl.maxpos / (4096ull * 4096ull) + 64, S.d_scratch);
-	const size_t per_group = (size_t)sp.np * ((size_t)C * sp.spc + 2 + (size_t)sp.px * sp.px) * sizeof(float) +
+	const size_t per_group = (size_t)sp.np * ((size_t)term_stride(C) * sp.spc + 2 + (size_t)sp.px * sp.px) * sizeof(float) +
 	                         (mode.learned ? (size_t)kMlpInPad * 2 + (size_t)kMlpOutN * 4 : 0);
 	size_t budget = ctx->slot_budget;
 	long long chunk = std::max<long long>(1, (long long)(budget / per_group));
@@ -507,7 +507,7 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	chunk = std::min<long long>(chunk, std::max<long long>(1, G));
 	S.chunk = chunk;
 	if (!mode.samples) {
-		DBUF("vals", (size_t)chunk * sp.np * C * sp.spc, S.d_vals);
+		DBUF("vals", (size_t)chunk * sp.np * term_stride(C) * sp.spc, S.d_vals);
 		DBUF("wslot", (size_t)chunk * sp.np, S.d_wslot);
 		DBUF("list", (size_t)chunk * sp.np, S.d_list);
 		DBUF("slist", (size_t)chunk * sp.np * sp.px * sp.px, S.d_sl);
@@ -672,7 +672,7 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 				const int t_lo = std::max(0, ta - reach);
 				const int t_hi = std::min((int)F - sp.pt, tb + reach);
 				CK(launch_gather(T, sp, t_lo, t_hi, S.d_off, S.d_list, S.d_soff, S.d_sl, S.d_scratch, S.d_vals,
-				                 S.d_wslot, S.d_win, S.d_acc + T.pix0 * C, S.d_wacc + T.pix0, st));
+				                 S.d_acc + T.pix0 * C, S.d_wacc + T.pix0, st));
 				ctx->launches += 4;
 			}
 		}
