@@ -501,20 +501,23 @@ gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *_
 #pragma unroll
 		for (int c = 0; c < CC; c++) a[c] = acc[((size_t)t * CC + c) * wh + xy];
 		float wa = wacc[pix];
-		for (;;) {
+		// the C estimates and the weight term of a term: one vector load
+		constexpr int TS = CC == 1 ? 2 : (CC <= 3 ? 4 : 8);
+		// terms are fetched D ahead of the one being added (a ring of D
+		// register slots, fetched and consumed in the same rotation), so that
+		// D loads of this pixel are in flight instead of one
+		constexpr int D = TS <= 4 ? 4 : 2;
+		auto fetch = [&](float (&x)[TS]) -> bool {
 			unsigned best = 0xffffffffu;
 			int bl = -1;
 #pragma unroll
 			for (int l = 0; l < L; l++)
 				if (head[l] < best) { best = head[l]; bl = l; }
-			if (bl < 0) break;
+			if (bl < 0) return false;
 			const unsigned slot = best >> 6;
 			const int dx = best & 7, dy = (best >> 3) & 7;
 			const int p = (bl * px + dy) * px + dx;
-			// the C estimates and the weight term of (slot, p): one vector load
-			constexpr int TS = CC == 1 ? 2 : (CC <= 3 ? 4 : 8);
 			const float *v = vals + ((size_t)slot * spc + p) * TS;
-			float x[TS];
 			if (TS == 2) {
 				const float2 q = __ldg(reinterpret_cast<const float2 *>(v));
 				x[0] = q.x;
@@ -536,9 +539,24 @@ gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *_
 					cur[l]++;
 					nxt[l] = cur[l] + 1 < end[l] ? __ldg(sl + cur[l] + 1) : 0xffffffffu;
 				}
+			return true;
+		};
+		float x[D][TS];
+		bool ok[D];
 #pragma unroll
-			for (int c = 0; c < CC; c++) a[c] = __fadd_rn(a[c], x[c]);
-			wa = __fadd_rn(wa, x[CC]);   // w * window[p], as the reference forms it
+		for (int d = 0; d < D; d++) ok[d] = fetch(x[d]);
+		bool live = true;
+		while (live) {
+#pragma unroll
+			for (int d = 0; d < D; d++) {
+				if (live && !ok[d]) live = false;
+				if (live) {
+#pragma unroll
+					for (int c = 0; c < CC; c++) a[c] = __fadd_rn(a[c], x[d][c]);
+					wa = __fadd_rn(wa, x[d][CC]);   // w * window[p], as the reference forms it
+					ok[d] = fetch(x[d]);
+				}
+			}
 		}
 		wacc[pix] = wa;
 #pragma unroll
