@@ -506,7 +506,7 @@ gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *_
 		// terms are fetched D ahead of the one being added (a ring of D
 		// register slots, fetched and consumed in the same rotation), so that
 		// D loads of this pixel are in flight instead of one
-		constexpr int D = TS <= 4 ? 4 : 2;
+		constexpr int D = TS == 2 ? 8 : (TS == 4 ? 4 : 2);
 		auto fetch = [&](float (&x)[TS]) -> bool {
 			unsigned best = 0xffffffffu;
 			int bl = -1;
