@@ -292,10 +292,10 @@ __device__ __forceinline__ void patch_distance2(const float *p0, const float *p1
 							for (int hx2 = 0; hx2 < (PX > 0 ? 1 : px); hx2++) {
 								const int xx = PX > 0 ? hx : hx2;
 								const float rv = (PX > 0 && PX % 4 == 0) ? rrow[xx % QV] : rf[xx];
-								const float d0 = __fsub_rn(rv, __ldg(p0 + off + xx));
-								const float d1 = __fsub_rn(rv, __ldg(p1 + off + xx));
-								a0 = __fadd_rn(a0, __fmul_rn(d0, d0));
-								a1 = __fadd_rn(a1, __fmul_rn(d1, d1));
+								float m0, m1;
+								sqdiff2(rv, rv, __ldg(p0 + off + xx), __ldg(p1 + off + xx), m0, m1);
+								a0 = __fadd_rn(a0, m0);
+								a1 = __fadd_rn(a1, m1);
 							}
 						}
 					}
