@@ -148,23 +148,27 @@ struct SelectShared {
 	float bound;
 	unsigned nsel;
 	int has_nan;        // a NaN distance: only the heap replay orders it as the reference does
-	float sd[kSelCap];
+	float sd[kSelCap];  // candidates under the bound, in no particular order
 	int si[kSelCap];
+	float od[kMaxNp];   // the K nearest, in partial_sort's order
+	int oi[kMaxNp];
 	float hd[kMaxNp];
 	int hi[kMaxNp];
 };
 
 // The k nearest of dist[0..ncand) in std::partial_sort's output order; the
-// first K entries of S.sd / S.si receive them, sorted.
+// first K entries of S.od / S.oi receive them, sorted.
 //
 // Fast path: every thread knows the minimum of the distances it computed; the
 // K-th smallest of those minima bounds the K-th smallest distance from above
 // (they are K distinct candidates).  All candidates under the bound are
-// compacted and one warp sorts them.  When the K smallest are pairwise
-// distinct and strictly below every other distance, partial_sort's output is
-// exactly this ascending order.  Otherwise (exact ties, or too many
-// candidates under the bound) warp 0 replays libstdc++'s heap selection
-// (__heap_select then __sort_heap) over the candidates in order.
+// compacted, and each takes its place in the output from its rank among them
+// (ties by candidate index), counted by its own thread.
+// When the K smallest are pairwise distinct and strictly below every other
+// distance, partial_sort's output is exactly this ascending order.
+// Otherwise (exact ties, a NaN, or too many candidates under the bound) warp
+// 0 replays libstdc++'s heap selection (__heap_select then __sort_heap) over
+// the candidates in order.
 __device__ void select_knn(const float *dist, int ncand, int K, float tmin, SelectShared &S)
 {
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -172,6 +176,7 @@ __device__ void select_knn(const float *dist, int ncand, int K, float tmin, Sele
 	if (tid == 0) {
 		S.nsel = 0u;
 		S.has_nan = 0;
+		S.bound = __int_as_float(0x7f800000);
 	}
 	__syncthreads();
 	if (warp == 0) {
@@ -214,48 +219,29 @@ __device__ void select_knn(const float *dist, int ncand, int K, float tmin, Sele
 	}
 	if (__syncthreads_or(nan) && tid == 0) S.has_nan = 1;
 	__syncthreads();
-	if (warp == 0) {
-		const int n = (int)S.nsel;
-		bool ok = n >= K && n <= kSelCap && !S.has_nan;
-		if (ok) {
-			// bitonic sort of up to 64 (distance, candidate) pairs, 2 per lane
-			float d0 = lane < n ? S.sd[lane] : __int_as_float(0x7f800000);
-			int i0 = lane < n ? S.si[lane] : 0x7fffffff;
-			float d1 = lane + 32 < n ? S.sd[lane + 32] : __int_as_float(0x7f800000);
-			int i1 = lane + 32 < n ? S.si[lane + 32] : 0x7fffffff;
-			// element e = lane + 32*h; compare-exchange across e ^ j
-			for (int k = 2; k <= 64; k <<= 1)
-				for (int j = k >> 1; j > 0; j >>= 1) {
-					if (j == 32) {
-						const bool up = (lane & k) == 0;   // k == 64 here: always ascending
-						const bool sw = up ? (d0 > d1 || (d0 == d1 && i0 > i1)) : (d0 < d1 || (d0 == d1 && i0 < i1));
-						if (sw) { float td = d0; d0 = d1; d1 = td; int ti = i0; i0 = i1; i1 = ti; }
-					} else {
-						const float od0 = __shfl_xor_sync(0xffffffffu, d0, j), od1 = __shfl_xor_sync(0xffffffffu, d1, j);
-						const int oi0 = __shfl_xor_sync(0xffffffffu, i0, j), oi1 = __shfl_xor_sync(0xffffffffu, i1, j);
-						const bool low = (lane & j) == 0;
-						const bool up0 = (lane & k) == 0, up1 = ((lane + 32) & k) == 0;
-						const bool t0 = (low == up0) ? (od0 < d0 || (od0 == d0 && oi0 < i0)) : (od0 > d0 || (od0 == d0 && oi0 > i0));
-						const bool t1 = (low == up1) ? (od1 < d1 || (od1 == d1 && oi1 < i1)) : (od1 > d1 || (od1 == d1 && oi1 > i1));
-						if (t0) { d0 = od0; i0 = oi0; }
-						if (t1) { d1 = od1; i1 = oi1; }
-					}
-				}
-			// checks on the sorted list e = 0..n-1: distinct among the first K,
-			// and the K-th strictly below the (K+1)-th
-			const float nd0 = __shfl_down_sync(0xffffffffu, d0, 1);
-			const float first1 = __shfl_sync(0xffffffffu, d1, 0);
-			const float nxt0 = lane == 31 ? first1 : nd0;           // element lane+1
-			const float nd1 = __shfl_down_sync(0xffffffffu, d1, 1);  // element lane+33
-			const bool bad0 = lane + 1 < n && lane < K && nxt0 == d0;
-			const bool bad1 = lane + 33 < n && lane + 32 < K && nd1 == d1;
-			ok = __ballot_sync(0xffffffffu, bad0 || bad1) == 0u;
-			if (ok) {
-				if (lane < K) { S.sd[lane] = d0; S.si[lane] = i0; }
-				if (lane + 32 < K) { S.sd[lane + 32] = d1; S.si[lane + 32] = i1; }
+	const int n = (int)S.nsel;
+	bool ok = n >= K && n <= kSelCap && !S.has_nan;
+	if (ok) {
+		// each selected candidate's rank among the selected, ties by index
+		int bad = 0;
+		if (tid < n) {
+			const float d = S.sd[tid];
+			const int ci = S.si[tid];
+			int rank = 0, same = 0;
+			for (int j = 0; j < n; j++) {
+				const float o = S.sd[j];
+				const int oj = S.si[j];
+				rank += (o < d || (o == d && oj < ci)) ? 1 : 0;
+				same += (o == d && j != tid) ? 1 : 0;
 			}
+			// one of the K nearest tied with another candidate: the heap decides
+			bad = rank < K && same > 0;
+			if (rank < K) { S.od[rank] = d; S.oi[rank] = ci; }
 		}
-		if (!ok) {
+		ok = !__syncthreads_or(bad);
+	}
+	if (!ok) {
+		if (warp == 0) {
 			// exact replay of libstdc++'s heap selection, candidates in order
 			float *hd = S.hd;
 			int *hi = S.hi;
@@ -280,11 +266,11 @@ __device__ void select_knn(const float *dist, int ncand, int K, float tmin, Sele
 			}
 			if (lane == 0) {
 				sort_heap(hd, hi, K);
-				for (int i = 0; i < K; i++) { S.sd[i] = hd[i]; S.si[i] = hi[i]; }
+				for (int i = 0; i < K; i++) { S.od[i] = hd[i]; S.oi[i] = hi[i]; }
 			}
 		}
+		__syncthreads();
 	}
-	__syncthreads();
 }
 
 // One CTA handles one group at a time: every thread computes column strips of
@@ -350,10 +336,10 @@ search_kernel(Image src, StepParams sp, SearchArgs a)
 		select_knn(dist, ncand, K, tmin, S);
 		// tau rule (nldct.cpp:1284-1289), then one thread per kept neighbour
 		int n = 1;
-		while (2 * n <= K && S.sd[n] < sp.tau2) n *= 2;
+		while (2 * n <= K && S.od[n] < sp.tau2) n *= 2;
 		if (tid == 0) a.nsimp[g] = (uint8_t)n;
 		if (tid < n) {
-			const int c = S.si[tid];
+			const int c = S.oi[tid];
 			int jj = 0;
 			while (jj + 1 < nframes && fw[jj + 1].cbase <= c) jj++;
 			const FrameWin &f = fw[jj];
