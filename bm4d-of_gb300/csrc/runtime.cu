@@ -1147,11 +1147,22 @@ bm4dof_status run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n, un
 		}
 		if (!X.fork) CK(cudaEventCreateWithFlags(&X.fork, cudaEventDisableTiming));
 		while (X.children.size() < n) X.children.push_back(make_child(ctx));
+		// every sequence holds its buffers for the whole graph: the chunk
+		// budgets of all of them together stay within half the device memory
+		size_t per_child = (size_t)(tu.slot_mb ? tu.slot_mb : 1024) << 20;
+		{
+			size_t freeb = 0, totalb = 0, held = 0;
+			for (bm4dof_ctx *c : X.children) held += c->held;
+			if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) {
+				const size_t cap = std::max<size_t>((size_t)64 << 20, (freeb + held) / 2 / n);
+				per_child = std::min(per_child, cap);
+			}
+		}
 		// allocation of every sequence's buffers, before the capture
 		for (unsigned i = 0; i < n; i++) {
 			bm4dof_ctx *c = X.children[i];
 			c->st = X.branches[i % nb];
-			c->slot_budget = (size_t)(tu.slot_mb ? tu.slot_mb : 1024) << 20;
+			c->slot_budget = per_child;
 			c->search_ctas = tu.search_ctas;
 			c->kappa = ctx->kappa;
 			c->has_gain = ctx->has_gain;
