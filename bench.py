@@ -48,7 +48,7 @@ WORKLOADS = {
 CLI = dict(px1=4, px2=4, pt1=4, pt2=4, wx1=21, wx2=21, np1=16, np2=16, b1=3.0)
 METRIC = "megapixel-frames/s at 1 GPU, plain vs learned/mixed at ≤0.05 dB PSNR loss"
 UNIT = "MPF/s"
-SEARCH_TRAFFIC_SMALL = 11.24e6 + 0.272e6
+SEARCH_TRAFFIC_SMALL = 11.24e6 + 0.648e6
 # CPU sample (crop of the same workload) for the host-core baseline
 CPU_SAMPLE = (480, 272, 13)
 
