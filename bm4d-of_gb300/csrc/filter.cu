@@ -341,6 +341,16 @@ __device__ __forceinline__ void quad_sync(int id)
 	asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(kQuadSub) : "memory");
 }
 
+// (x0 * y0, x1 * y1), each rounded as __fmul_rn (mul.rn.f32x2)
+__device__ __forceinline__ void mul2(float x0, float x1, float y0, float y1, float &p0, float &p1)
+{
+	unsigned long long x, y, z;
+	asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(x0), "f"(x1));
+	asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(y0), "f"(y1));
+	asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(z) : "l"(x), "l"(y));
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(p0), "=f"(p1) : "l"(z));
+}
+
 // out[(q0 + c) * nsp + n0 + m] = sum_r in[r * nsp + n0 + m] * M[r * 64 + q0 + c]
 __device__ __forceinline__ void product4x4(const float *in, const float *M, float *out, int nsp, int q0, int n0)
 {
@@ -353,11 +363,23 @@ __device__ __forceinline__ void product4x4(const float *in, const float *M, floa
 	for (int r = 0; r < 64; r++) {
 		const float4 g = *reinterpret_cast<const float4 *>(in + r * nsp + n0);
 		const float4 b = *reinterpret_cast<const float4 *>(M + r * 64 + q0);
-		const float gm[4] = {g.x, g.y, g.z, g.w}, bc[4] = {b.x, b.y, b.z, b.w};
+		// the 16 products as 8 packed multiplies of member pairs (m, m+1) by
+		// coefficient pairs taken straight and swapped; each sum still takes
+		// one rounded add per term in r order (a packed multiply whose lanes
+		// are added one at a time rounds exactly as the scalar pair)
+		float p[4][4];
+		mul2(g.x, g.y, b.x, b.y, p[0][0], p[1][1]);
+		mul2(g.x, g.y, b.y, b.x, p[0][1], p[1][0]);
+		mul2(g.x, g.y, b.z, b.w, p[0][2], p[1][3]);
+		mul2(g.x, g.y, b.w, b.z, p[0][3], p[1][2]);
+		mul2(g.z, g.w, b.x, b.y, p[2][0], p[3][1]);
+		mul2(g.z, g.w, b.y, b.x, p[2][1], p[3][0]);
+		mul2(g.z, g.w, b.z, b.w, p[2][2], p[3][3]);
+		mul2(g.z, g.w, b.w, b.z, p[2][3], p[3][2]);
 #pragma unroll
 		for (int m = 0; m < 4; m++)
 #pragma unroll
-			for (int c = 0; c < 4; c++) a[m][c] = __fadd_rn(a[m][c], __fmul_rn(gm[m], bc[c]));
+			for (int c = 0; c < 4; c++) a[m][c] = __fadd_rn(a[m][c], p[m][c]);
 	}
 #pragma unroll
 	for (int c = 0; c < 4; c++)
