@@ -166,7 +166,7 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
                     const float *__restrict__ win, long long g_begin, long long g_end,
                     const uint8_t *__restrict__ nsimp, const uint32_t *__restrict__ idx,
                     const uint8_t *__restrict__ alive, float *__restrict__ vals,
-                    float *__restrict__ wslot, float *__restrict__ wgroup, uint8_t *__restrict__ eq)
+                    float *__restrict__ wgroup, uint8_t *__restrict__ eq)
 {
 	extern __shared__ __align__(16) float sm[];
 	const int px = PX ? PX : sp.px, pt = PT ? PT : sp.pt, C = CC ? CC : sp.C;
@@ -321,7 +321,6 @@ filter_exact_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, in
 			const int n = it / spc, p = it % spc;
 			vals[((slot0 + n) * spc + p) * ts + C] = __fmul_rn(w, wn[p]);
 		}
-		if (tid < ns) wslot[slot0 + tid] = w;
 		if (tid == 0) { wgroup[g] = w; eq[g] = 0; }
 	}
 }
@@ -392,7 +391,7 @@ filter_quad_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, int
                    const float *__restrict__ basis, const float *__restrict__ binv, const float *__restrict__ win,
                    long long g_begin, long long g_end, const uint8_t *__restrict__ nsimp,
                    const uint32_t *__restrict__ idx, const uint8_t *__restrict__ alive, float *__restrict__ vals,
-                   float *__restrict__ wslot, float *__restrict__ wgroup, uint8_t *__restrict__ eq)
+                   float *__restrict__ wgroup, uint8_t *__restrict__ eq)
 {
 	constexpr int SPC = PX * PX * PT;
 	static_assert(SPC == 64, "four-group filter: 64-element patches");
@@ -503,7 +502,6 @@ filter_quad_kernel(Image noisy, Image basic, const Tile *__restrict__ tiles, int
 		const float wp = __fmul_rn(wg, wn[t]);
 		for (int n = 0; n < ns; n++)
 			reinterpret_cast<float2 *>(vals)[(slot0 + n) * SPC + t] = make_float2(__fmul_rn(wp, Gn[t * nsp + n]), wp);
-		if (t < ns) wslot[slot0 + t] = wg;
 		if (t == 0) { wgroup[g] = wg; eq[g] = 0; }
 		quad_sync(bar);
 	}
@@ -518,7 +516,7 @@ __global__ void fixup_equal_kernel(const Tile *__restrict__ tiles, int ntiles, S
                                    const float *__restrict__ win, long long g_begin, long long g_end,
                                    const uint8_t *__restrict__ nsimp, const uint8_t *__restrict__ alive,
                                    const uint8_t *__restrict__ eq, const float *__restrict__ wgroup,
-                                   float *__restrict__ vals, float *__restrict__ wslot)
+                                   float *__restrict__ vals)
 {
 	const int per = sp.C * sp.spc;
 	for (long long g = g_begin + blockIdx.x * (long long)blockDim.x + threadIdx.x; g < g_end;
@@ -531,7 +529,6 @@ __global__ void fixup_equal_kernel(const Tile *__restrict__ tiles, int ntiles, S
 			float w = 1.f;
 			for (long long q = g - 1; q >= T.g0; q--)
 				if (alive[q] && !eq[q] && nsimp[q] > n) { w = wgroup[q]; break; }
-			wslot[slot0 + n] = w;
 			const int ts = term_stride(sp.C);
 			float *v = vals + (slot0 + n) * sp.spc * ts;
 			for (int p = 0; p < sp.spc; p++) {
@@ -559,14 +556,14 @@ template <int STEP, int PX, int PT, int CC>
 cudaError_t launch_exact(int blocks, size_t smem, cudaStream_t st, const Image &noisy, const Image &basic,
                          const Tile *tiles, int ntiles, const StepParams &sp, const float *basis, const float *binv,
                          const float *win, long long g_begin, long long g_end, const uint8_t *nsimp,
-                         const uint32_t *idx, const uint8_t *alive, float *vals, float *wslot, float *wgroup,
+                         const uint32_t *idx, const uint8_t *alive, float *vals, float *wgroup,
                          uint8_t *eq)
 {
 	auto kern = filter_exact_kernel<STEP, PX, PT, CC>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
 	kern<<<blocks, kFilterThreads, smem, st>>>(noisy, basic, tiles, ntiles, sp, basis, binv, win, g_begin, g_end,
-	                                          nsimp, idx, alive, vals, wslot, wgroup, eq);
+	                                          nsimp, idx, alive, vals, wgroup, eq);
 	return cudaGetLastError();
 }
 
@@ -574,23 +571,23 @@ template <int STEP, int PX, int PT>
 cudaError_t launch_quad(int blocks, size_t smem, cudaStream_t st, const Image &noisy, const Image &basic,
                         const Tile *tiles, int ntiles, const StepParams &sp, const float *basis, const float *binv,
                         const float *win, long long g_begin, long long g_end, const uint8_t *nsimp,
-                        const uint32_t *idx, const uint8_t *alive, float *vals, float *wslot, float *wgroup,
+                        const uint32_t *idx, const uint8_t *alive, float *vals, float *wgroup,
                         uint8_t *eq)
 {
 	auto kern = filter_quad_kernel<STEP, PX, PT>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
 	kern<<<blocks, kQuadSub * kQuadGroups, smem, st>>>(noisy, basic, tiles, ntiles, sp, basis, binv, win, g_begin,
-	                                                  g_end, nsimp, idx, alive, vals, wslot, wgroup, eq);
+	                                                  g_end, nsimp, idx, alive, vals, wgroup, eq);
 	return cudaGetLastError();
 }
 
 #define FILTER_ARGS_NB noisy, basic, tiles, ntiles, sp, basis, binv, win, g_begin, g_end, nsimp, idx, alive, vals, \
-	    wslot, wgroup, eq
+	    wgroup, eq
 
 #define FILTER_ARGS                                                                                   \
 	blocks, smem, st, noisy, basic, tiles, ntiles, sp, basis, binv, win, g_begin, g_end, nsimp, idx, alive, \
-	    vals, wslot, wgroup, eq
+	    vals, wgroup, eq
 
 }  // namespace
 
@@ -598,7 +595,7 @@ cudaError_t launch_filter(const Image &noisy, const Image &basic, const Tile *ti
                           const StepParams &sp, const float *basis, const float *binv,
                           const float *win, long long g_begin, long long g_end,
                           const uint8_t *nsimp, const uint32_t *idx, const uint8_t *alive,
-                          float *vals, float *wslot, float *wgroup, uint8_t *eq, int nsm,
+                          float *vals, float *wgroup, uint8_t *eq, int nsm,
                           cudaStream_t st)
 {
 	if (g_end <= g_begin) return cudaSuccess;
@@ -625,7 +622,7 @@ cudaError_t launch_filter(const Image &noisy, const Image &basic, const Tile *ti
 	if (e != cudaSuccess) return e;
 	const int fb = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
 	fixup_equal_kernel<<<fb, 256, 0, st>>>(tiles, ntiles, sp, win, g_begin, g_end, nsimp, alive, eq,
-	                                       wgroup, vals, wslot);
+	                                       wgroup, vals);
 	return cudaGetLastError();
 }
 

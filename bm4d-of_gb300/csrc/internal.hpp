@@ -51,7 +51,7 @@ cudaError_t launch_filter(const Image &noisy, const Image &basic, const Tile *ti
                           const StepParams &sp, const float *basis, const float *binv,
                           const float *win, long long g_begin, long long g_end,
                           const uint8_t *nsimp, const uint32_t *idx, const uint8_t *alive,
-                          float *vals, float *wslot, float *wgroup, uint8_t *eq, int nsm,
+                          float *vals, float *wgroup, uint8_t *eq, int nsm,
                           cudaStream_t st);
 
 // aggregate.cu
@@ -122,7 +122,7 @@ struct LearnedArgs {
 	const float *basis, *binv, *win;
 	__nv_bfloat16 *feat;                 // features: [rows][80]
 	const float *gains;                  // apply: [rows][64], or null (no network)
-	float *vals, *wslot;                 // apply: aggregation terms and weights
+	float *vals;                         // apply: aggregation terms (estimate, weight term)
 	float kappa;                         // apply: residual-variance fallback threshold
 	unsigned *nfallback;
 	float *sfeat, *starget;              // samples: [G][65], [G][64]

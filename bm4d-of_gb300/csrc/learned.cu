@@ -237,7 +237,6 @@ __device__ void group_body(const LearnedArgs &a, const StepParams &sp, long long
 #pragma unroll
 	for (int m = 0; m < NS; m++)
 		reinterpret_cast<float2 *>(a.vals)[(slot0 + m) * kSpc + k] = make_float2(wp * est[m], wp);
-	if (k < NS) a.wslot[slot0 + k] = wgt;
 }
 
 template <int MODE>
@@ -464,7 +463,6 @@ __device__ void tc_group(const LearnedArgs &a, const StepParams &sp, long long g
 		for (int m = 0; m < NS; m++)
 			reinterpret_cast<float2 *>(a.vals)[(slot0 + m) * kSpc + p] = make_float2(wp * W.Z[p][m], wp);
 	}
-	if (lane < NS) a.wslot[slot0 + lane] = wgt;
 }
 
 template <int MODE>

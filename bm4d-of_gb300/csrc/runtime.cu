@@ -309,7 +309,7 @@ struct StepState {
 	unsigned *d_small = nullptr;          // [0] edges, [3] fallbacks, [64..] per-tile counts
 	long long *d_blocks = nullptr;
 	unsigned long long *d_edges = nullptr;
-	float *d_acc = nullptr, *d_wacc = nullptr, *d_vals = nullptr, *d_wslot = nullptr;
+	float *d_acc = nullptr, *d_wacc = nullptr, *d_vals = nullptr;
 	unsigned *d_cnt = nullptr, *d_off = nullptr, *d_soff = nullptr, *d_scratch = nullptr, *d_list = nullptr,
 	         *d_sl = nullptr;
 	__nv_bfloat16 *d_lfeat = nullptr;
@@ -499,7 +499,7 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	DBUF("off", pl.maxpos + 1, S.d_off);
 	DBUF("soff", pl.maxpos + 1, S.d_soff);
 	DBUF("scratch", pl.maxpos / 4096 + pl.maxpos / (4096ull * 4096ull) + 64, S.d_scratch);
-	const size_t per_group = (size_t)sp.np * ((size_t)term_stride(C) * sp.spc + 2 + (size_t)sp.px * sp.px) * sizeof(float) +
+	const size_t per_group = (size_t)sp.np * ((size_t)term_stride(C) * sp.spc + 1 + (size_t)sp.px * sp.px) * sizeof(float) +
 	                         (mode.learned ? (size_t)kMlpInPad * 2 + (size_t)kMlpOutN * 4 : 0);
 	size_t budget = ctx->slot_budget;
 	long long chunk = std::max<long long>(1, (long long)(budget / per_group));
@@ -508,7 +508,6 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	S.chunk = chunk;
 	if (!mode.samples) {
 		DBUF("vals", (size_t)chunk * sp.np * term_stride(C) * sp.spc, S.d_vals);
-		DBUF("wslot", (size_t)chunk * sp.np, S.d_wslot);
 		DBUF("list", (size_t)chunk * sp.np, S.d_list);
 		DBUF("slist", (size_t)chunk * sp.np * sp.px * sp.px, S.d_sl);
 	}
@@ -640,7 +639,6 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 					la.gb = gb;
 					la.feat = S.d_lfeat;
 					la.vals = S.d_vals;
-					la.wslot = S.d_wslot;
 					la.gains = nullptr;
 					if (ctx->has_gain) {
 						CK(launch_learned(kLearnedFeatures, la, sp, ctx->nsm, st));
@@ -653,7 +651,7 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 					ctx->launches++;
 				} else {
 					CK(launch_filter(noisy, basic, S.d_tiles, ntiles, sp, S.d_basis, S.d_binv, S.d_win, ga, gb,
-					                 S.d_nsimp, S.d_idx, S.d_alive, S.d_vals, S.d_wslot, S.d_wgroup, S.d_eq,
+					                 S.d_nsimp, S.d_idx, S.d_alive, S.d_vals, S.d_wgroup, S.d_eq,
 					                 ctx->nsm, st));
 					ctx->launches += 2;
 				}
