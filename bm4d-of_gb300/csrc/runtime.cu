@@ -764,17 +764,27 @@ void free_child(bm4dof_ctx *c)
 	delete c;
 }
 
+// Rows of W floats to or from the padded device pitch P; with no padding the
+// video is one contiguous copy (one large DMA instead of H*C*F row copies).
 bm4dof_status upload(bm4dof_ctx *ctx, const Image &dst, const float *src)
 {
-	CK(cudaMemcpy2DAsync(dst.p, sizeof(float) * dst.P, src, sizeof(float) * dst.W, sizeof(float) * dst.W,
-	                     (size_t)dst.H * dst.C * dst.F, cudaMemcpyDefault, ctx->st));
+	const size_t rows = (size_t)dst.H * dst.C * dst.F;
+	if (dst.P == dst.W)
+		CK(cudaMemcpyAsync(dst.p, src, sizeof(float) * dst.W * rows, cudaMemcpyDefault, ctx->st));
+	else
+		CK(cudaMemcpy2DAsync(dst.p, sizeof(float) * dst.P, src, sizeof(float) * dst.W, sizeof(float) * dst.W, rows,
+		                     cudaMemcpyDefault, ctx->st));
 	return BM4DOF_OK;
 }
 
 bm4dof_status download(bm4dof_ctx *ctx, float *dst, const Image &src)
 {
-	CK(cudaMemcpy2DAsync(dst, sizeof(float) * src.W, src.p, sizeof(float) * src.P, sizeof(float) * src.W,
-	                     (size_t)src.H * src.C * src.F, cudaMemcpyDefault, ctx->st));
+	const size_t rows = (size_t)src.H * src.C * src.F;
+	if (src.P == src.W)
+		CK(cudaMemcpyAsync(dst, src.p, sizeof(float) * src.W * rows, cudaMemcpyDefault, ctx->st));
+	else
+		CK(cudaMemcpy2DAsync(dst, sizeof(float) * src.W, src.p, sizeof(float) * src.P, sizeof(float) * src.W, rows,
+		                     cudaMemcpyDefault, ctx->st));
 	return BM4DOF_OK;
 }
 
