@@ -41,3 +41,24 @@ def test_no_cpu_fallback_when_library_missing(tmp_path):
         raise AssertionError("loading a missing library must fail")
     finally:
         mod._lib = None
+
+
+def test_flag_values_match_the_header(gpulib):
+    """The Python binding's run flags are the header's #define values."""
+    import pyoracle
+    text = open(os.path.join(ROOT, "include", "bm4dof.h")).read()
+    flags = {m.group(1): int(m.group(2), 16) for m in re.finditer(r"#define BM4DOF_([A-Z0-9_]+)\s+0x([0-9a-fA-F]+)u", text)}
+    for name in ("DEVICE_POINTERS", "KEEP_GROUPS", "MIXED_PRECISION", "LEARNED", "VBM3D_SEARCH"):
+        assert getattr(gpulib, name) == flags[name], name
+    assert pyoracle.VBM3D_SEARCH == flags["VBM3D_SEARCH"]
+
+
+def test_cli_params_take_the_predictive_search_options(gpulib, oracle):
+    """bm4dof.cli_params resolves -wxf/-npf/-dsub/-t like the reference's VBM3D_SEARCH build."""
+    from helpers import resolve_params
+    kw = dict(px1=4, np1=16, wxf1=7, wxf2=3, npf1=3, npf2=4, dsub1=2.5, dsub2=0.0, t1=40.0, t2=12.0)
+    a = gpulib.cli_params((40, 36, 6, 1), 20.0, **kw)
+    b = resolve_params(oracle, (40, 36, 6, 1), 20.0, **kw)
+    for pa, pb in zip(a, b):
+        for f, _ in gpulib.Params._fields_:
+            assert getattr(pa, f) == getattr(pb, f), f

@@ -138,3 +138,42 @@ def test_gpu_vbm3d_rejections(gpulib, gpuctx):
     p1.nSimilarPatchesPred = 30   # more than a 5x5 predicted window holds
     with pytest.raises(gpulib.BM4DOFError, match="fewer positions"):
         gpuctx.runNlBayes(g["noisy"], g["fflow"], g["bflow"], p1, p2, nparts=2, vbm3d=True)
+
+
+@pytest.mark.parametrize("seed,nparts,cfg,vbm3d", [
+    (311, 6, dict(CFG_VIDEO, paste_boost=True), False),
+    (312, 4, dict(CFG_VIDEO, paste_boost=True), True),
+    (313, 2, dict(CFG_VIDEO, order_inv=True), True),
+    (314, 2, dict(CFG_VIDEO, paste_boost=True, order_inv=True), False),
+])
+def test_gpu_paste_and_predictive_combinations(gpulib, gpuctx, oracle, seed, nparts, cfg, vbm3d):
+    """The paste trick and the predictive search with more tiles and with
+    order-invariant filtering, against the oracle (both pinned to the
+    reference separately)."""
+    W, H, F = 52, 40, 6
+    clean, nz, ff, bf = video_case(W, H, F, sigma=20.0, seed=seed)
+    po = resolve_params(oracle, (W, H, F, 1), 20.0, **cfg)
+    pg = resolve_params(gpulib, (W, H, F, 1), 20.0, **cfg)
+    ob, of, orat, tr = oracle.runNlBayes(nz, ff, bf, *po, nparts=nparts, nthreads=1, trace_cap=100000,
+                                         trace_stride=32, vbm3d=vbm3d)
+    gb, gf, grat = gpuctx.runNlBayes(nz, ff, bf, *pg, nparts=nparts, keep_groups=True, vbm3d=vbm3d)
+    same_groups(gpuctx, tr, nparts)
+    assert np.array_equal(gb, ob, equal_nan=True) and np.array_equal(gf, of, equal_nan=True) and grat == orat
+
+
+def test_gpu_paste_batched_matches_golden(gpulib, gpuctx):
+    import torch
+    g = dict(np.load(os.path.join(GOLDEN, "video_paste.npz")))
+    p1, p2 = gparams(gpulib, g["p1"]), gparams(gpulib, g["p2"])
+    dev = torch.device("cuda", 0)
+    items = []
+    for k in range(2):
+        nz = torch.from_numpy(g["noisy"]).to(dev)
+        items.append(dict(noisy=nz, fflow=torch.from_numpy(g["fflow"]).to(dev),
+                          bflow=torch.from_numpy(g["bflow"]).to(dev), basic=torch.empty_like(nz),
+                          final=torch.empty_like(nz), p1=p1, p2=p2, nparts=2))
+    ratios = gpuctx.run_batched(items)
+    for it, r in zip(items, ratios):
+        assert np.array_equal(it["basic"].cpu().numpy(), g["basic"])
+        assert np.array_equal(it["final"].cpu().numpy(), g["final"])
+        assert r == tuple(g["ratios"].tolist())
