@@ -1,6 +1,6 @@
 """Mixed-precision form: FP16 tensor-core pre-screen of the patch distances and
 an exact FP32 re-rank of the best 2k candidates.  Not bit-exact by design; the
-checks are the spec bars: neighbour sets that agree with the exact path
+checks are the bars of the mixed form: neighbour sets that agree with the exact path
 (the selected k nearest match whenever the true k nearest are among the 2k
 best approximations) and a PSNR loss of at most 0.05 dB against the plain
 method."""
