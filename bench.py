@@ -122,6 +122,21 @@ def dist_env():
     return rank, world, local
 
 
+def replica_max_ms(ms, world):
+    """The slowest rank's time: every rank is an independent replica of the
+    whole workload (no data exchange), so the job takes as long as its slowest
+    replica.  The reduction runs on the process group's own device (CUDA
+    tensors for NCCL, host tensors for gloo)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_baseline(nz, ff, bf, sigma, threads=None, sample=CPU_SAMPLE):
     """The reference algorithm on the host cores (oracle restatement, OpenMP over
     the reference's 2*threads tiles) on a crop of the workload."""
@@ -329,11 +344,7 @@ def main():
             launches += n
         barrier()
         wall = time.perf_counter() - t0
-    dev_ms = sum(totals)
-    if world > 1:
-        t = torch.tensor([dev_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(t.item())
+    dev_ms = replica_max_ms(sum(totals), world)
     ms_step = dev_ms / args.steps
     mpf = W * H * F / 1e6
     value = world * mpf / (ms_step / 1e3)
@@ -348,7 +359,7 @@ def main():
         ms, _ = step_host()
         e2e_ms.append(ms[4])
     barrier()
-    e2e_value = world * mpf / (statistics.mean(e2e_ms) / 1e3)
+    e2e_value = world * mpf / (replica_max_ms(statistics.mean(e2e_ms), world) / 1e3)
 
     if rank != 0:
         return 0
