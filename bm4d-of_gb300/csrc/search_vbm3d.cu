@@ -258,47 +258,40 @@ __device__ __forceinline__ void patch_distance2(const float *p0, const float *p1
                                                 const float *ref, int reps, int px_rt, int pt_rt, float &a0,
                                                 float &a1)
 {
+	// compile-time extents when the shape is a template argument (full
+	// unrolling of a row), run-time ones otherwise
 	const int px = PX > 0 ? PX : px_rt, pt = PX > 0 ? PT : pt_rt, spc = px * px * pt;
+	constexpr bool VEC = PX > 0 && PX % 4 == 0;   // reference rows as 16-byte loads
+	constexpr int QV = VEC ? PX : 4;
 	a0 = 0.f;
 	a1 = 0.f;
 	for (int r = 0; r < reps; r++) {
 		const float *rr = ref + r * spc;
-		// one patch frame unrolled at a time (bounded register use)
+		// one patch frame at a time (bounded register use)
 #pragma unroll 1
-		for (int ht = 0; ht < (PX > 0 ? PT : 1); ht++) {
-			for (int ht2 = 0; ht2 < (PX > 0 ? 1 : pt); ht2++) {
-				const int tt = PX > 0 ? ht : ht2;
+		for (int tt = 0; tt < pt; tt++) {
 #pragma unroll
-				for (int hy = 0; hy < (PX > 0 ? PX : 1); hy++) {
-					for (int hy2 = 0; hy2 < (PX > 0 ? 1 : px); hy2++) {
-						const int yy = PX > 0 ? hy : hy2;
-						const size_t off = tt * tpitch + yy * rpitch;
-						const float *rf = rr + (tt * px + yy) * px;
-						// the reference row from shared memory in 16-byte loads
-						constexpr int QV = (PX > 0 && PX % 4 == 0) ? PX : 4;
-						float rrow[QV];
-						if (PX > 0 && PX % 4 == 0) {
+			for (int yy = 0; yy < (PX > 0 ? PX : px); yy++) {
+				const size_t off = tt * tpitch + yy * rpitch;
+				const float *rf = rr + (tt * px + yy) * px;
+				float rrow[QV];
+				if (VEC) {
 #pragma unroll
-							for (int q = 0; q < QV / 4; q++) {
-								const float4 r4 = reinterpret_cast<const float4 *>(rf)[q];
-								rrow[4 * q] = r4.x;
-								rrow[4 * q + 1] = r4.y;
-								rrow[4 * q + 2] = r4.z;
-								rrow[4 * q + 3] = r4.w;
-							}
-						}
-#pragma unroll
-						for (int hx = 0; hx < (PX > 0 ? PX : 1); hx++) {
-							for (int hx2 = 0; hx2 < (PX > 0 ? 1 : px); hx2++) {
-								const int xx = PX > 0 ? hx : hx2;
-								const float rv = (PX > 0 && PX % 4 == 0) ? rrow[xx % QV] : rf[xx];
-								float m0, m1;
-								sqdiff2(rv, rv, __ldg(p0 + off + xx), __ldg(p1 + off + xx), m0, m1);
-								a0 = __fadd_rn(a0, m0);
-								a1 = __fadd_rn(a1, m1);
-							}
-						}
+					for (int q = 0; q < QV / 4; q++) {
+						const float4 r4 = reinterpret_cast<const float4 *>(rf)[q];
+						rrow[4 * q] = r4.x;
+						rrow[4 * q + 1] = r4.y;
+						rrow[4 * q + 2] = r4.z;
+						rrow[4 * q + 3] = r4.w;
 					}
+				}
+#pragma unroll
+				for (int xx = 0; xx < (PX > 0 ? PX : px); xx++) {
+					const float rv = VEC ? rrow[xx % QV] : rf[xx];
+					float m0, m1;
+					sqdiff2(rv, rv, __ldg(p0 + off + xx), __ldg(p1 + off + xx), m0, m1);
+					a0 = __fadd_rn(a0, m0);
+					a1 = __fadd_rn(a1, m1);
 				}
 			}
 		}
