@@ -11,7 +11,8 @@
  * reference compiled with -ffp-contract=off and the project's sequential
  * sgemm (oracle/ref_sgemm.c).  Parity pinning: tests compare this file's
  * output with the reference itself (oracle/_ref, built from the reference
- * sources by oracle/build_ref.sh) and with fixtures under tests/golden/.
+ * sources by `make -C oracle ref`, also with its VBM3D_SEARCH switch) and
+ * with fixtures under tests/golden/.
  *
  * Build: g++ -std=c++17 -O3 -ffp-contract=off -fopenmp -shared -fPIC
  */

@@ -2,8 +2,10 @@
  * ref_harness.cpp -- TEST INFRASTRUCTURE ONLY.
  *
  * C entry points around the reference's own, unmodified VideoNLB code
- * (src/core/nldct.cpp et al., compiled in place by oracle/build_ref.sh into
- * oracle/_ref/libbm4dof_ref.so).  Videos are built in memory; no file I/O.
+ * (src/core/nldct.cpp et al., compiled in place by `make -C oracle ref` into
+ * oracle/_ref/libbm4dof_ref.so, and with the reference's VBM3D_SEARCH switch
+ * into oracle/_ref/libbm4dof_ref_vbm3d.so).  Videos are built in memory; no
+ * file I/O.
  * Used to pin the oracle restatement (oracle/bm4dof_oracle.cpp) and to
  * generate tests/golden fixtures.
  */
