@@ -312,6 +312,27 @@ __device__ __forceinline__ void window_box(int cx, int cy, int sw, int tw, int t
 	ny = max(0, min(th - px, cy + hw - shy) - y0 + 1);
 }
 
+// The sizeSearchWindowPred window of frame qt around a match `id` (tile
+// index) of frame qt - dir, moved along the flow at the match, rounded half
+// away from zero and clamped to the tile (nldct.cpp:978-993).
+__device__ __forceinline__ void predicted_window(const Image &ffl, const Image &bfl, const Tile &T,
+                                                 const StepParams &sp, uint32_t id, int qt, int dir, int &x0,
+                                                 int &y0, int &nx, int &ny)
+{
+	const int cx0 = (int)(id % (uint32_t)T.w);
+	const int cy0 = (int)((id / (uint32_t)T.w) % (uint32_t)T.h);
+	const int ct0 = qt - dir;
+	float ux = 0.f, uy = 0.f;
+	if (sp.use_flow) {
+		const Image &fl = dir > 0 ? ffl : bfl;
+		ux = fl.p[fl.at(T.ox + cx0, T.oy + cy0, ct0, 0)];
+		uy = fl.p[fl.at(T.ox + cx0, T.oy + cy0, ct0, 1)];
+	}
+	const int cx = (int)fmaxf(0.f, fminf(__fsub_rn((float)T.w, 1.f), roundf(__fadd_rn((float)cx0, ux))));
+	const int cy = (int)fmaxf(0.f, fminf(__fsub_rn((float)T.h, 1.f), roundf(__fadd_rn((float)cy0, uy))));
+	window_box(cx, cy, sp.wxp, T.w, T.h, sp.px, x0, y0, nx, ny);
+}
+
 template <int PX, int PT, int MINB>
 __global__ void __launch_bounds__(32 * kWarps, MINB)
 search_vbm3d_kernel(Image src, Image ffl, Image bfl, StepParams sp, VArgs a)
@@ -382,21 +403,8 @@ search_vbm3d_kernel(Image src, Image ffl, Image bfl, StepParams sp, VArgs a)
 				const int dir = qt > t ? 1 : -1;
 				const int prev = (qt == t - 1) ? 0 : ii - 1;
 				int bx0 = 0, by0 = 0, bnx = 0, bny = 0;
-				if (lane < npf) {
-					const uint32_t id = pool_i[prev * npf + lane];
-					const int cx0 = (int)(id % (uint32_t)T.w);
-					const int cy0 = (int)((id / (uint32_t)T.w) % (uint32_t)T.h);
-					const int ct0 = qt - dir;
-					float ux = 0.f, uy = 0.f;
-					if (sp.use_flow) {
-						const Image &fl = dir > 0 ? ffl : bfl;
-						ux = fl.p[fl.at(T.ox + cx0, T.oy + cy0, ct0, 0)];
-						uy = fl.p[fl.at(T.ox + cx0, T.oy + cy0, ct0, 1)];
-					}
-					const int cx = (int)fmaxf(0.f, fminf(__fsub_rn((float)T.w, 1.f), roundf(__fadd_rn((float)cx0, ux))));
-					const int cy = (int)fmaxf(0.f, fminf(__fsub_rn((float)T.h, 1.f), roundf(__fadd_rn((float)cy0, uy))));
-					window_box(cx, cy, sp.wxp, T.w, T.h, px, bx0, by0, bnx, bny);
-				}
+				if (lane < npf)
+					predicted_window(ffl, bfl, T, sp, pool_i[prev * npf + lane], qt, dir, bx0, by0, bnx, bny);
 				// union of the windows in window, then raster order
 				ncand = 0;
 				for (int w = 0; w < npf; w++) {
@@ -474,21 +482,8 @@ search_vbm3d_kernel(Image src, Image ffl, Image bfl, StepParams sp, VArgs a)
 				const int slot = h == 0 ? k : nf + k;
 				const int prev = h == 0 ? k - 1 : (k == 1 ? 0 : nf + k - 1);
 				int bx0 = 0, by0 = 0, bnx = 0, bny = 0;
-				if (act && hl < npf) {
-					const uint32_t id = pool_i[prev * npf + hl];
-					const int cx0 = (int)(id % (uint32_t)T.w);
-					const int cy0 = (int)((id / (uint32_t)T.w) % (uint32_t)T.h);
-					const int ct0 = qt - dir;
-					float ux = 0.f, uy = 0.f;
-					if (sp.use_flow) {
-						const Image &fl = dir > 0 ? ffl : bfl;
-						ux = fl.p[fl.at(T.ox + cx0, T.oy + cy0, ct0, 0)];
-						uy = fl.p[fl.at(T.ox + cx0, T.oy + cy0, ct0, 1)];
-					}
-					const int cx = (int)fmaxf(0.f, fminf(__fsub_rn((float)T.w, 1.f), roundf(__fadd_rn((float)cx0, ux))));
-					const int cy = (int)fmaxf(0.f, fminf(__fsub_rn((float)T.h, 1.f), roundf(__fadd_rn((float)cy0, uy))));
-					window_box(cx, cy, sp.wxp, T.w, T.h, px, bx0, by0, bnx, bny);
-				}
+				if (act && hl < npf)
+					predicted_window(ffl, bfl, T, sp, pool_i[prev * npf + hl], qt, dir, bx0, by0, bnx, bny);
 				// each half's union, 16 positions per ballot
 				int cnt = 0;
 				for (int w = 0; w < npf; w++) {
