@@ -109,6 +109,23 @@ __device__ __forceinline__ void merge32(float &ld, int &lc, float nd, int nc)
 	}
 }
 
+// Insert (nd, nc) into the sorted 32-list held one per lane when it beats
+// the last entry: lanes after its place shift up by one.
+__device__ __forceinline__ void insert32(float &ld, int &lc, float nd, int nc)
+{
+	const int lane = threadIdx.x & 31;
+	const float lastd = __shfl_sync(0xffffffffu, ld, 31);
+	const int lastc = __shfl_sync(0xffffffffu, lc, 31);
+	if (!better(nd, nc, lastd, lastc)) return;
+	const int at = __popc(__ballot_sync(0xffffffffu, better(ld, lc, nd, nc)));
+	const float ud = __shfl_up_sync(0xffffffffu, ld, 1);
+	const int uc = __shfl_up_sync(0xffffffffu, lc, 1);
+	if (lane > at) { ld = ud; lc = uc; }
+	else if (lane == at) { ld = nd; lc = nc; }
+}
+
+constexpr int kInsertMax = 8;   // newcomers inserted one by one; more: one bitonic merge
+
 struct MixedArgs {
 	const Tile *tiles;
 	int ntiles;
@@ -330,8 +347,20 @@ search_mixed_kernel(Image src, StepParams sp, MixedArgs a)
 					const float th = __shfl_sync(0xffffffffu, ld, 31);
 					const int i = i0 + lane;
 					const float d = i < nw ? dist(r, i) : __int_as_float(0x7f800000);
-					if (__ballot_sync(0xffffffffu, i < nw && d < th) == 0u) continue;
-					merge32(ld, lc, i < nw ? d : __int_as_float(0x7f800000), i < nw ? base + i : 0x7fffffff);
+					unsigned m = __ballot_sync(0xffffffffu, i < nw && d < th);
+					if (m == 0u) continue;
+					if (__popc(m) > kInsertMax) {
+						merge32(ld, lc, i < nw ? d : __int_as_float(0x7f800000), i < nw ? base + i : 0x7fffffff);
+						continue;
+					}
+					// few newcomers: insert them one at a time (same list)
+					while (m) {
+						const int j = __ffs(m) - 1;
+						m &= m - 1u;
+						const float dj = __shfl_sync(0xffffffffu, d, j);
+						const int cj = base + i0 + j;
+						insert32(ld, lc, dj, cj);
+					}
 				}
 				s_ld[r][lane] = ld;
 				s_lc[r][lane] = lc;
