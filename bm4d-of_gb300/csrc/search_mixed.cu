@@ -124,7 +124,7 @@ __device__ __forceinline__ void insert32(float &ld, int &lc, float nd, int nc)
 	else if (lane == at) { ld = nd; lc = nc; }
 }
 
-constexpr int kInsertMax = 8;   // newcomers inserted one by one; more: one bitonic merge
+constexpr int kInsertMax = 16;  // newcomers inserted one by one; more: one bitonic merge
 
 struct MixedArgs {
 	const Tile *tiles;
