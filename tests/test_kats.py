@@ -125,3 +125,42 @@ def test_color_transform_roundtrip(oracle):
         assert np.allclose((y.astype(np.float64) ** 2).sum(1), (v.astype(np.float64) ** 2).sum(1), rtol=1e-5)
     g = rng.uniform(0, 255, size=(2, 1, 5, 7)).astype(np.float32)
     assert np.array_equal(oracle.color_transform(g, True), g)
+
+
+def _shifted_window(c, sw, extent, px):
+    """nldct.cpp:1248-1258: the window is shifted, not clipped, into the frame."""
+    hw = (sw - 1) // 2
+    sh = min(0, c - hw) + max(0, c + hw - extent + px)
+    return max(0, c - hw - sh), min(extent - px, c + hw - sh)
+
+
+@pytest.mark.parametrize("vbm3d", [False, True])
+def test_neighbours_lie_in_the_shifted_window(oracle, vbm3d):
+    # one frame, no flow: every neighbour of a reference patch lies in its
+    # search window, which keeps its full size at the borders (shifted)
+    import pyoracle
+    from helpers import resolve_params, video_case
+    W, H = 40, 34
+    clean, nz, ff, bf = video_case(W, H, 1, sigma=20.0, seed=7)
+    cfg = dict(px1=8, px2=8, pt1=1, pt2=1, wx1=21, wx2=21, np1=16, np2=16)
+    p1, p2 = resolve_params(oracle, (W, H, 1, 1), 20.0, **cfg)
+    _, _, _, tr = oracle.runNlBayes(nz, None, None, p1, p2, nparts=1, trace_cap=100000, trace_stride=32,
+                                    vbm3d=vbm3d)
+    assert tr["count"] > 0
+    for ref, ns, idx in zip(tr["ref"], tr["nsimp"], tr["index"]):
+        x, y = int(ref) % W, int(ref) // W
+        x0, x1 = _shifted_window(x, 21, W, 8)
+        y0, y1 = _shifted_window(y, 21, H, 8)
+        assert x1 - x0 + 1 == 21 and y1 - y0 + 1 == 21
+        for q in idx[:ns]:
+            qx, qy = int(q) % W, int(q) // W
+            assert x0 <= qx <= x1 and y0 <= qy <= y1
+
+
+def test_shifted_window_known_answers():
+    # at the left border, in the middle, at the right border (W=40, px=8, 21 wide)
+    assert _shifted_window(0, 21, 40, 8) == (0, 20)
+    assert _shifted_window(16, 21, 40, 8) == (6, 26)
+    assert _shifted_window(39, 21, 40, 8) == (12, 32)
+    # a window wider than the frame's positions is clipped to them
+    assert _shifted_window(5, 41, 40, 8) == (0, 32)
