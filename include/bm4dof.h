@@ -223,9 +223,11 @@ typedef struct bm4dof_tuning {
 	unsigned search_ctas;  /* exact search CTAs per SM: 4 or 6; 0: 6             */
 } bm4dof_tuning;
 
-/* Denoises n sequences (flags: BM4DOF_MIXED_PRECISION, BM4DOF_LEARNED; the
- * pointers are always device pointers).  tuning may be NULL (defaults).
- * bm4dof_last_timings reports the graph launch as ms[4]. */
+/* Denoises n sequences (flags: BM4DOF_MIXED_PRECISION, BM4DOF_LEARNED,
+ * BM4DOF_VBM3D_SEARCH; the pointers are always device pointers).  tuning may
+ * be NULL (defaults).  Each sequence's chunk budget is capped so that all the
+ * sequences' buffers fit in half the device memory.  bm4dof_last_timings
+ * reports the graph launch as ms[4]. */
 bm4dof_status bm4dof_run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n, unsigned flags,
                                  const bm4dof_tuning *tuning);
 
