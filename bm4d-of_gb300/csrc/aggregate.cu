@@ -99,32 +99,6 @@ kill_fixpoint_kernel(const unsigned long long *__restrict__ edges, const unsigne
 	}
 }
 
-__global__ void kill_mark_kernel(const unsigned long long *__restrict__ edges, unsigned n,
-                                 const uint8_t *__restrict__ alive, uint8_t *__restrict__ killed,
-                                 int clear)
-{
-	for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-		const unsigned long long v = edges[e];
-		const long long u = (long long)(v >> 32), w = (long long)(v & 0xffffffffull);
-		if (clear) killed[w] = 0;
-		else if (alive[u]) killed[w] = 1;
-	}
-}
-
-__global__ void kill_apply_kernel(const unsigned long long *__restrict__ edges, unsigned n,
-                                  const uint8_t *__restrict__ killed, uint8_t *__restrict__ alive,
-                                  unsigned *__restrict__ changed)
-{
-	for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-		const long long w = (long long)(edges[e] & 0xffffffffull);
-		const uint8_t a = killed[w] ? 0 : 1;
-		if (alive[w] != a) {
-			alive[w] = a;
-			*changed = 1u;
-		}
-	}
-}
-
 // Paste trick (doPasteBoost, nldct.cpp:2302-2322 and 2395-2415): a
 // processed group switches off every member's position and its four
 // neighbours outside the border band of 2*sPx (linear offsets -w, +w, -1, +1,
@@ -675,16 +649,6 @@ cudaError_t launch_kill_edges(const Tile *tiles, int ntiles, const int *grid, co
                               unsigned long long *edges, unsigned *nedges, unsigned cap, cudaStream_t st)
 {
 	kill_edges_kernel<<<grid_for(G, 256, 8192), 256, 0, st>>>(tiles, ntiles, grid, inv, sp, G, idx, edges, nedges, cap);
-	return cudaGetLastError();
-}
-
-cudaError_t launch_kill_iteration(const unsigned long long *edges, unsigned n, uint8_t *alive, uint8_t *killed,
-                                  unsigned *changed, cudaStream_t st)
-{
-	const int b = grid_for(n, 256, 8192);
-	kill_mark_kernel<<<b, 256, 0, st>>>(edges, n, alive, killed, 1);
-	kill_mark_kernel<<<b, 256, 0, st>>>(edges, n, alive, killed, 0);
-	kill_apply_kernel<<<b, 256, 0, st>>>(edges, n, killed, alive, changed);
 	return cudaGetLastError();
 }
 

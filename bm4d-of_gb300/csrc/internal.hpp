@@ -59,8 +59,6 @@ cudaError_t launch_kill_edges(const Tile *tiles, int ntiles, const int *grid, co
                               const StepParams &sp, long long G, const uint32_t *idx,
                               unsigned long long *edges, unsigned *nedges, unsigned cap,
                               cudaStream_t st);
-cudaError_t launch_kill_iteration(const unsigned long long *edges, unsigned n, uint8_t *alive,
-                                  uint8_t *killed, unsigned *changed, cudaStream_t st);
 // Switch-offs resolved on the device in one launch (no host round trip).
 cudaError_t launch_kill_fixpoint(const unsigned long long *edges, const unsigned *nedges, unsigned cap,
                                  uint8_t *alive, uint8_t *killed, cudaStream_t st);
