@@ -63,11 +63,11 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    cli_src = os.path.join(SRC, "cli.cpp")
-    hdr = os.path.join(HERE, "..", "include", "bm4dof.h")
-    if not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(x) for x in (cli_src, hdr, LIB)):
+    cli_src = [os.path.join(SRC, "cli.cpp"), os.path.join(SRC, "frames.cpp")]
+    deps = cli_src + [os.path.join(SRC, "frames.hpp"), os.path.join(HERE, "..", "include", "bm4dof.h"), LIB]
+    if not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(x) for x in deps):
         cxx = shutil.which("g++") or "g++"
-        cmd = [cxx, "-O2", "-std=c++17", cli_src, "-o", CLI, "-L" + OUT, "-lbm4dof_gpu",
+        cmd = [cxx, "-O2", "-std=c++17", *cli_src, "-o", CLI, "-L" + OUT, "-lbm4dof_gpu",
                "-Wl,-rpath,$ORIGIN"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -5,17 +5,7 @@
 // Frame files are addressed by printf patterns with -f/-l/-s exactly as
 // Video<float>::loadVideo / saveVideo do (src/utils/lib_videot.cpp:30-126).
 //
-// File formats (the reference reads and writes through iio; this build reads
-// and writes the float formats itself and has no image libraries):
-//   .pfm  Portable Float Map: "Pf" grey or "PF" three channels, rows stored
-//         bottom to top, little endian when the scale is negative;
-//   .flo  Middlebury optical flow: "PIEH", int32 width and height, then
-//         interleaved (u, v) float32 pixels, top row first (the layout iio
-//         reads, lib/iio/iio.c:1885-1903);
-//   .png  output only: 8-bit grey or RGB, values rounded and clamped to
-//         [0, 255], stored (uncompressed) deflate blocks.
-// As the reference's loadImage does (src/utils/lib_image.cpp:66-73), a
-// three-channel frame whose channels are all equal is read as grey.
+// Frame files (PFM, TIFF, .flo, PNG) are read and written by frames.cpp.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -26,6 +16,10 @@
 #include <vector>
 
 #include "../../include/bm4dof.h"
+#include "frames.hpp"
+
+using bm4dof_frames::read_frame;
+using bm4dof_frames::write_frame;
 
 namespace {
 
@@ -69,212 +63,6 @@ struct Args {
 		if (help) std::printf("    %-12s = %-16s : %s\n", n, d, use);
 	}
 };
-
-// ---- frame files -------------------------------------------------------------
-bool ends_with(const std::string &s, const char *e)
-{
-	const size_t n = std::strlen(e);
-	return s.size() >= n && !s.compare(s.size() - n, n, e);
-}
-
-bool host_little_endian()
-{
-	const uint16_t v = 1;
-	unsigned char b[2];
-	std::memcpy(b, &v, 2);
-	return b[0] == 1;
-}
-
-void swap4(unsigned char *p)
-{
-	std::swap(p[0], p[3]);
-	std::swap(p[1], p[2]);
-}
-
-// planar (c, y, x) floats
-bool read_pfm(const char *path, std::vector<float> &out, int &w, int &h, int &c)
-{
-	FILE *f = std::fopen(path, "rb");
-	if (!f) return false;
-	char tag[3] = {0, 0, 0};
-	float scale = 0.f;
-	bool ok = std::fscanf(f, "%2s %d %d %f", tag, &w, &h, &scale) == 4 && w > 0 && h > 0;
-	if (ok) ok = std::fgetc(f) != EOF;   // the single whitespace before the data
-	c = tag[1] == 'F' ? 3 : 1;
-	ok = ok && tag[0] == 'P' && (tag[1] == 'F' || tag[1] == 'f');
-	std::vector<unsigned char> raw;
-	if (ok) {
-		raw.resize((size_t)w * h * c * 4);
-		ok = std::fread(raw.data(), 1, raw.size(), f) == raw.size();
-	}
-	std::fclose(f);
-	if (!ok) return false;
-	const bool swap = (scale < 0.f) != host_little_endian();
-	out.assign((size_t)w * h * c, 0.f);
-	for (int y = 0; y < h; y++)
-		for (int x = 0; x < w; x++)
-			for (int k = 0; k < c; k++) {
-				unsigned char *p = &raw[(((size_t)(h - 1 - y) * w + x) * c + k) * 4];   // bottom row first
-				if (swap) swap4(p);
-				std::memcpy(&out[((size_t)k * h + y) * w + x], p, 4);
-			}
-	return true;
-}
-
-bool write_pfm(const char *path, const float *planar, int w, int h, int c)
-{
-	FILE *f = std::fopen(path, "wb");
-	if (!f) return false;
-	std::fprintf(f, "%s\n%d %d\n%s\n", c == 3 ? "PF" : "Pf", w, h, host_little_endian() ? "-1.0" : "1.0");
-	std::vector<float> row((size_t)w * c);
-	bool ok = true;
-	for (int y = h - 1; y >= 0 && ok; y--) {
-		for (int x = 0; x < w; x++)
-			for (int k = 0; k < c; k++) row[(size_t)x * c + k] = planar[((size_t)k * h + y) * w + x];
-		ok = std::fwrite(row.data(), sizeof(float), row.size(), f) == row.size();
-	}
-	return std::fclose(f) == 0 && ok;
-}
-
-bool read_flo(const char *path, std::vector<float> &out, int &w, int &h, int &c)
-{
-	FILE *f = std::fopen(path, "rb");
-	if (!f) return false;
-	float magic = 0.f;
-	int32_t wh[2] = {0, 0};
-	bool ok = std::fread(&magic, 4, 1, f) == 1 && std::fread(wh, 4, 2, f) == 2 && magic == 202021.25f &&
-	          wh[0] > 0 && wh[1] > 0;
-	w = wh[0];
-	h = wh[1];
-	c = 2;
-	std::vector<float> raw;
-	if (ok) {
-		raw.resize((size_t)w * h * 2);
-		ok = std::fread(raw.data(), sizeof(float), raw.size(), f) == raw.size();
-	}
-	std::fclose(f);
-	if (!ok) return false;
-	out.assign(raw.size(), 0.f);
-	for (size_t p = 0; p < (size_t)w * h; p++) {
-		out[p] = raw[2 * p];
-		out[(size_t)w * h + p] = raw[2 * p + 1];
-	}
-	return true;
-}
-
-bool write_flo(const char *path, const float *planar, int w, int h)
-{
-	FILE *f = std::fopen(path, "wb");
-	if (!f) return false;
-	const float magic = 202021.25f;
-	const int32_t wh[2] = {w, h};
-	std::vector<float> raw((size_t)w * h * 2);
-	for (size_t p = 0; p < (size_t)w * h; p++) {
-		raw[2 * p] = planar[p];
-		raw[2 * p + 1] = planar[(size_t)w * h + p];
-	}
-	bool ok = std::fwrite(&magic, 4, 1, f) == 1 && std::fwrite(wh, 4, 2, f) == 2 &&
-	          std::fwrite(raw.data(), sizeof(float), raw.size(), f) == raw.size();
-	return std::fclose(f) == 0 && ok;
-}
-
-uint32_t crc32(const unsigned char *p, size_t n, uint32_t c = 0xffffffffu)
-{
-	for (size_t i = 0; i < n; i++) {
-		c ^= p[i];
-		for (int k = 0; k < 8; k++) c = (c >> 1) ^ (0xedb88320u & (0u - (c & 1u)));
-	}
-	return c;
-}
-
-void put32(std::vector<unsigned char> &v, uint32_t x)
-{
-	for (int s = 24; s >= 0; s -= 8) v.push_back((unsigned char)(x >> s));
-}
-
-bool write_png(const char *path, const float *planar, int w, int h, int c)
-{
-	// scanlines: filter byte 0, then 8-bit samples
-	const int cc = c == 3 ? 3 : 1;
-	std::vector<unsigned char> raw;
-	raw.reserve((size_t)h * (w * cc + 1));
-	for (int y = 0; y < h; y++) {
-		raw.push_back(0);
-		for (int x = 0; x < w; x++)
-			for (int k = 0; k < cc; k++) {
-				float v = std::round(planar[((size_t)k * h + y) * w + x]);
-				v = v < 0.f ? 0.f : (v > 255.f ? 255.f : v);
-				raw.push_back((unsigned char)v);
-			}
-	}
-	// zlib stream of stored blocks
-	std::vector<unsigned char> z = {0x78, 0x01};
-	uint32_t a = 1, b = 0;
-	for (unsigned char ch : raw) {
-		a = (a + ch) % 65521u;
-		b = (b + a) % 65521u;
-	}
-	for (size_t o = 0; o < raw.size() || raw.empty();) {
-		const size_t n = std::min<size_t>(65535, raw.size() - o);
-		const bool last = o + n == raw.size();
-		z.push_back(last ? 1 : 0);
-		z.push_back((unsigned char)(n & 0xff));
-		z.push_back((unsigned char)(n >> 8));
-		z.push_back((unsigned char)(~n & 0xff));
-		z.push_back((unsigned char)((~n >> 8) & 0xff));
-		z.insert(z.end(), raw.begin() + o, raw.begin() + o + n);
-		o += n;
-		if (last) break;
-	}
-	put32(z, (b << 16) | a);
-	std::vector<unsigned char> png = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
-	auto chunk = [&png](const char *type, const std::vector<unsigned char> &data) {
-		put32(png, (uint32_t)data.size());
-		std::vector<unsigned char> td(type, type + 4);
-		td.insert(td.end(), data.begin(), data.end());
-		png.insert(png.end(), td.begin(), td.end());
-		put32(png, crc32(td.data(), td.size()) ^ 0xffffffffu);
-	};
-	std::vector<unsigned char> ihdr;
-	put32(ihdr, (uint32_t)w);
-	put32(ihdr, (uint32_t)h);
-	ihdr.push_back(8);
-	ihdr.push_back(cc == 3 ? 2 : 0);
-	ihdr.push_back(0);
-	ihdr.push_back(0);
-	ihdr.push_back(0);
-	chunk("IHDR", ihdr);
-	chunk("IDAT", z);
-	chunk("IEND", {});
-	FILE *f = std::fopen(path, "wb");
-	if (!f) return false;
-	const bool ok = std::fwrite(png.data(), 1, png.size(), f) == png.size();
-	return std::fclose(f) == 0 && ok;
-}
-
-bool read_frame(const char *path, std::vector<float> &out, int &w, int &h, int &c)
-{
-	const std::string p(path);
-	bool ok = ends_with(p, ".flo") ? read_flo(path, out, w, h, c) : read_pfm(path, out, w, h, c);
-	if (ok && c == 3) {   // equal channels: grey (lib_image.cpp:66-73)
-		const size_t wh = (size_t)w * h;
-		size_t k = 0;
-		while (k < wh && out[k] == out[wh + k] && out[k] == out[2 * wh + k]) k++;
-		if (k == wh) {
-			out.resize(wh);
-			c = 1;
-		}
-	}
-	return ok;
-}
-
-bool write_frame(const char *path, const float *planar, int w, int h, int c)
-{
-	const std::string p(path);
-	if (ends_with(p, ".flo")) return c == 2 && write_flo(path, planar, w, h);
-	if (ends_with(p, ".png")) return write_png(path, planar, w, h, c);
-	return write_pfm(path, planar, w, h, c);
-}
 
 struct Video {
 	std::vector<float> data;

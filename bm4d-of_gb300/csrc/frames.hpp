@@ -1,0 +1,30 @@
+// frames.hpp -- frame files of the command line (host code, no GPU).
+//
+// The reference reads and writes frames through iio (lib/iio); this build has
+// no image libraries and reads and writes the formats its scripts use itself:
+//   .pfm        Portable Float Map: "Pf" grey or "PF" three channels, rows
+//               bottom to top, little endian when the scale is negative;
+//   .tif/.tiff  baseline TIFF, uncompressed: read with 8-, 16- or 32-bit
+//               unsigned integer or 32-bit float samples, 1 to 4 per pixel,
+//               interleaved or planar, in strips, either byte order (values
+//               taken as they are, as iio does); written as 32-bit float,
+//               little endian, interleaved, one strip;
+//   .flo        Middlebury optical flow: "PIEH", int32 width and height, then
+//               interleaved (u, v) float32 pixels, top row first (the layout
+//               iio reads, lib/iio/iio.c:1885-1903);
+//   .png        output only: 8-bit grey or RGB, values rounded and clamped to
+//               [0, 255], stored (uncompressed) deflate blocks.
+// Any other extension is read and written as PFM.  As the reference's
+// loadImage does (src/utils/lib_image.cpp:66-73), a three-channel frame whose
+// channels are all equal is read as grey.  Frames are planar (c, y, x) floats.
+#pragma once
+
+#include <string>
+#include <vector>
+
+namespace bm4dof_frames {
+
+bool read_frame(const char *path, std::vector<float> &out, int &w, int &h, int &c);
+bool write_frame(const char *path, const float *planar, int w, int h, int c);
+
+}  // namespace bm4dof_frames
