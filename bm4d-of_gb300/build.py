@@ -20,6 +20,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libbm4dof_gpu.so")
 CLI = os.path.join(OUT, "bm4dof")          # the command line, linked to LIB
+TVL1_CLI = os.path.join(OUT, "tvl1flow")   # the optical-flow command line, linked to LIB
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
@@ -39,7 +40,8 @@ def nvcc() -> str:
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
     path = os.path.join(SRC, src)
-    deps = [path] + [os.path.join(SRC, h) for h in os.listdir(SRC) if h.endswith((".cuh", ".hpp", ".h"))]
+    deps = [path] + [os.path.join(SRC, h) for h in os.listdir(SRC)
+                     if h.endswith((".cuh", ".hpp", ".h")) and h != "frames.hpp"]
     deps.append(os.path.join(HERE, "..", "include", "bm4dof.h"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
@@ -54,6 +56,22 @@ def _compile(src: str, verbose: bool) -> str:
     return obj
 
 
+def _link_cli(main_src: str, exe: str) -> None:
+    """A command line over LIB: main_src plus the frame files, host code only
+    (no contraction, so the double arithmetic of the colour reduction rounds
+    alike on every host)."""
+    src = [os.path.join(SRC, main_src), os.path.join(SRC, "frames.cpp")]
+    deps = src + [os.path.join(SRC, "frames.hpp"), os.path.join(HERE, "..", "include", "bm4dof.h"), LIB]
+    if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(x) for x in deps):
+        return
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", *src, "-o", exe, "-L" + OUT, "-lbm4dof_gpu",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{os.path.basename(exe)} build failed:\n{r.stdout}\n{r.stderr}")
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
@@ -63,15 +81,8 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    cli_src = [os.path.join(SRC, "cli.cpp"), os.path.join(SRC, "frames.cpp")]
-    deps = cli_src + [os.path.join(SRC, "frames.hpp"), os.path.join(HERE, "..", "include", "bm4dof.h"), LIB]
-    if not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(x) for x in deps):
-        cxx = shutil.which("g++") or "g++"
-        cmd = [cxx, "-O2", "-std=c++17", *cli_src, "-o", CLI, "-L" + OUT, "-lbm4dof_gpu",
-               "-Wl,-rpath,$ORIGIN"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"cli build failed:\n{r.stdout}\n{r.stderr}")
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        list(ex.map(lambda a: _link_cli(*a), [("cli.cpp", CLI), ("tvl1_cli.cpp", TVL1_CLI)]))
     return LIB
 
 

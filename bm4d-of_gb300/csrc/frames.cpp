@@ -224,7 +224,9 @@ struct TiffReader {
 	}
 };
 
-bool read_tiff(const char *path, std::vector<float> &out, int &w, int &h, int &c)
+// *sample (if given) receives the sample type: 8, 16 or 32 for unsigned
+// integers, 0 for 32-bit float
+bool read_tiff(const char *path, std::vector<float> &out, int &w, int &h, int &c, int *sample = nullptr)
 {
 	FILE *f = std::fopen(path, "rb");
 	if (!f) return false;
@@ -270,6 +272,7 @@ bool read_tiff(const char *path, std::vector<float> &out, int &w, int &h, int &c
 	w = (int)width;
 	h = (int)height;
 	c = (int)spp;
+	if (sample) *sample = fmt == 3 ? 0 : (int)bits;
 	const size_t bytes = bits / 8, wh = (size_t)w * h;
 	// the strips, in order, hold the samples in file order
 	std::vector<unsigned char> data;
@@ -373,6 +376,46 @@ bool read_frame(const char *path, std::vector<float> &out, int &w, int &h, int &
 		}
 	}
 	return ok;
+}
+
+bool read_grey(const char *path, std::vector<float> &out, int &w, int &h, std::string &why)
+{
+	const std::string p(path);
+	const bool tif = ends_with(p, ".tif") || ends_with(p, ".tiff") || ends_with(p, ".TIF") || ends_with(p, ".TIFF");
+	int c = 0, sample = 0;
+	std::vector<float> in;
+	const bool ok = ends_with(p, ".flo") ? read_flo(path, in, w, h, c)
+	                : tif                ? read_tiff(path, in, w, h, c, &sample)
+	                                     : read_pfm(path, in, w, h, c);
+	if (!ok) {
+		why = "could not read image";
+		return false;
+	}
+	if (c == 1) {
+		out.swap(in);
+		return true;
+	}
+	// iio_hacky_uncolorize / _uncolorizea (lib/iio/iio.c:935-1006): 8-bit and
+	// float samples with or without alpha, 16-bit without
+	if (!(c == 3 || c == 4) || sample == 32 || (c == 4 && sample == 16)) {
+		why = c == 3 || c == 4 ? "uncolorize type not supported" : "non-scalarizable image";
+		return false;
+	}
+	const size_t wh = (size_t)w * h;
+	out.resize(wh);
+	for (size_t i = 0; i < wh; i++) {
+		const double r = .299 * (double)in[i] + .587 * (double)in[wh + i] + .114 * (double)in[2 * wh + i];
+		out[i] = sample == 8 ? (float)(uint8_t)r : sample == 16 ? (float)(uint16_t)r : (float)r;
+	}
+	return true;
+}
+
+bool write_flow(const char *path, const float *uv, int w, int h)
+{
+	const std::string p(path);
+	if (ends_with(p, ".tif") || ends_with(p, ".tiff") || ends_with(p, ".TIF") || ends_with(p, ".TIFF"))
+		return write_tiff(path, uv, w, h, 2);
+	return write_flo(path, uv, w, h);
 }
 
 bool write_frame(const char *path, const float *planar, int w, int h, int c)

@@ -27,4 +27,17 @@ namespace bm4dof_frames {
 bool read_frame(const char *path, std::vector<float> &out, int &w, int &h, int &c);
 bool write_frame(const char *path, const float *planar, int w, int h, int c);
 
+// One grey frame as the reference's optical-flow tool reads it
+// (iio_read_image_float, lib/iio/iio.c:3486-3505): three channels become
+// .299 r + .587 g + .114 b, and four (colour and alpha) the same of the first
+// three, computed in double and stored in the file's sample type -- so
+// truncated for integer samples -- before the conversion to float.  Other
+// channel counts, and sample types iio does not reduce (32-bit integers, 16-bit
+// with alpha), are refused with the reason in why.
+bool read_grey(const char *path, std::vector<float> &out, int &w, int &h, std::string &why);
+
+// A flow field (u plane, then v plane) as the optical-flow tool saves it: a
+// two-channel float TIFF for .tif/.tiff names, Middlebury .flo for any other.
+bool write_flow(const char *path, const float *uv, int w, int h);
+
 }  // namespace bm4dof_frames

@@ -2,8 +2,9 @@
 the CPU through a small converter built from the same source: baseline TIFF in
 every sample layout the reference's scripts may hand it (8/16/32-bit integer
 and 32-bit float, 1 or 3 samples, interleaved or planar, several strips,
-either byte order), the float TIFF it writes, PFM, and the grey rule for
-three equal channels."""
+either byte order), the float TIFF it writes, PFM, the grey rule for three
+equal channels, and the optical-flow tool's reader (iio_read_image_float:
+colour reduced to grey in the file's sample type) and flow writer."""
 import os
 import shutil
 import struct
@@ -21,7 +22,7 @@ def convert(tmp_path_factory):
     if cxx is None:
         pytest.skip("g++ not available")
     exe = tmp_path_factory.mktemp("frames") / "frames_convert"
-    r = subprocess.run([cxx, "-O1", "-std=c++17", os.path.join(ROOT, "tests", "frames_convert.cpp"),
+    r = subprocess.run([cxx, "-O1", "-std=c++17", "-ffp-contract=off", os.path.join(ROOT, "tests", "frames_convert.cpp"),
                         os.path.join(ROOT, "bm4d-of_gb300", "csrc", "frames.cpp"), "-o", str(exe)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -152,3 +153,64 @@ def test_rejects_compressed_and_missing(convert, tmp_path):
     open(src, "wb").write(bytes(b))
     assert subprocess.run([convert, str(src), str(tmp_path / "o.pfm")]).returncode == 3
     assert subprocess.run([convert, str(tmp_path / "missing.tif"), str(tmp_path / "o.pfm")]).returncode == 3
+
+
+def iio_grey(planar, dtype):
+    """iio_hacky_uncolorize(a) (lib/iio/iio.c:935-1006): .299 r + .587 g + .114 b
+    in double, stored in the sample type (integers truncate), then float."""
+    r, g, b = (planar[k].astype(np.float64) for k in range(3))
+    return ((.299 * r + .587 * g) + .114 * b).astype(dtype).astype(np.float32)
+
+
+@pytest.mark.parametrize("dtype,channels", [(np.uint8, 3), (np.uint16, 3), (np.float32, 3),
+                                            (np.uint8, 4), (np.float32, 4)])
+def test_flow_tool_reads_colour_as_grey(convert, tmp_path, dtype, channels):
+    rng = np.random.default_rng(3)
+    hi = 256 if dtype == np.uint8 else 4000
+    img = rng.integers(0, hi, size=(channels, 11, 15)).astype(dtype)
+    img[:3, 0, :4] = hi - 1                      # white: the sum of the weights rounds below 1
+    if dtype == np.float32:
+        img = (img + rng.uniform(-0.5, 0.5, size=img.shape)).astype(np.float32)
+    src, dst = tmp_path / "c.tif", tmp_path / "g.pfm"
+    write_tiff(src, img, dtype, interleaved=channels == 3)
+    r = subprocess.run([convert, "-grey", str(src), str(dst)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split() == ["15", "11", "1"]
+    want = iio_grey(img, dtype)
+    assert np.array_equal(read_pfm(dst)[0], want)
+    if dtype != np.float32:
+        # truncation, not rounding: some pixels land one below the rounded value
+        exact = .299 * img[0].astype(np.float64) + .587 * img[1] + .114 * img[2]
+        assert np.all(want <= np.round(exact)) and np.any(want < np.round(exact))
+
+
+def test_flow_tool_reader_keeps_grey_and_refuses_the_rest(convert, tmp_path):
+    g = np.arange(20, dtype=np.float32).reshape(1, 4, 5) * 3.5
+    src, dst = tmp_path / "g.tif", tmp_path / "g.pfm"
+    write_tiff(src, g, np.float32)
+    assert subprocess.run([convert, "-grey", str(src), str(dst)], capture_output=True).returncode == 0
+    assert np.array_equal(read_pfm(dst), g)
+    for dtype, channels, why in [(np.uint32, 3, "uncolorize type not supported"),
+                                 (np.uint16, 4, "uncolorize type not supported"),
+                                 (np.float32, 2, "non-scalarizable image")]:
+        write_tiff(src, np.ones((channels, 4, 5), dtype), dtype)
+        r = subprocess.run([convert, "-grey", str(src), str(dst)], capture_output=True, text=True)
+        assert r.returncode == 3 and why in r.stderr, (dtype, channels, r.stderr)
+    r = subprocess.run([convert, "-grey", str(tmp_path / "missing.pfm"), str(dst)], capture_output=True, text=True)
+    assert r.returncode == 3 and "could not read image" in r.stderr
+
+
+def test_flow_written_as_flo_or_tiff(convert, tmp_path):
+    rng = np.random.default_rng(4)
+    uv = rng.normal(0, 3, size=(2, 6, 9)).astype(np.float32)
+    src = tmp_path / "in.flo"
+    with open(src, "wb") as f:
+        f.write(struct.pack("<fii", 202021.25, 9, 6))
+        f.write(np.ascontiguousarray(uv.transpose(1, 2, 0), "<f4").tobytes())
+    for name in ["out.flo", "out.other"]:        # any name but .tif/.tiff is .flo
+        dst = tmp_path / name
+        assert subprocess.run([convert, "-flow", str(src), str(dst)], capture_output=True).returncode == 0
+        assert open(dst, "rb").read() == open(src, "rb").read()
+    dst = tmp_path / "out.tif"
+    assert subprocess.run([convert, "-flow", str(src), str(dst)], capture_output=True).returncode == 0
+    assert np.array_equal(read_float_tiff(dst), uv)
