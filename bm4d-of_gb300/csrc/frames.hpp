@@ -1,6 +1,6 @@
 // frames.hpp -- frame files of the command line (host code, no GPU).
 //
-// The reference reads and writes frames through iio (lib/iio); this build has
+// The reference reads and writes frames through iio (lib/iio); this library has
 // no image libraries and reads and writes the formats its scripts use itself:
 //   .pfm        Portable Float Map: "Pf" grey or "PF" three channels, rows
 //               bottom to top, little endian when the scale is negative;

@@ -34,7 +34,7 @@ typedef enum bm4dof_status {
 	BM4DOF_ERR_NO_STEP = 5,       /* nldct.cpp:334  both patch sizes are zero      */
 	BM4DOF_ERR_BASIC_SIZE = 6,    /* nldct.cpp:341  basic size differs from noisy  */
 	BM4DOF_ERR_BIOR_SIZE = 7,     /* nldct.cpp:634  bior1.5 with patch size != 8   */
-	BM4DOF_ERR_UNSUPPORTED = 8,   /* parameter combination this build rejects      */
+	BM4DOF_ERR_UNSUPPORTED = 8,   /* parameter combination the library rejects     */
 	BM4DOF_ERR_CUDA = 9,          /* CUDA runtime error (message has the details)  */
 	BM4DOF_ERR_NO_MEMORY = 10,    /* device or host allocation failed              */
 	BM4DOF_ERR_TIMEOUT = 11,      /* a bounded device-side wait ran out            */
