@@ -21,6 +21,7 @@ OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libbm4dof_gpu.so")
 CLI = os.path.join(OUT, "bm4dof")          # the command line, linked to LIB
 TVL1_CLI = os.path.join(OUT, "tvl1flow")   # the optical-flow command line, linked to LIB
+CLI_ALIAS = os.path.join(OUT, "bm4d-of")   # the name the reference's scripts call the CLI by
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
@@ -83,6 +84,8 @@ def build(verbose: bool = False) -> str:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
         list(ex.map(lambda a: _link_cli(*a), [("cli.cpp", CLI), ("tvl1_cli.cpp", TVL1_CLI)]))
+    if not os.path.lexists(CLI_ALIAS):
+        os.symlink(os.path.basename(CLI), CLI_ALIAS)
     return LIB
 
 

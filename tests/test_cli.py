@@ -70,6 +70,13 @@ def test_cli_print_params(cli, oracle):
     assert r.stdout == oracle.formatNlbParameters(p1) + oracle.formatNlbParameters(p2)
 
 
+def test_cli_under_the_scripts_name(cli):
+    # scripts/bm4dof.sh runs "$DIR/bm4d-of"; the build provides that name too
+    alias = os.path.join(os.path.dirname(cli), "bm4d-of")
+    r = run(alias, "-i", "unused", "-print-prms", 1, "-sigma", 20)
+    assert r.returncode == 0 and r.stdout == run(cli, "-i", "unused", "-print-prms", 1, "-sigma", 20).stdout
+
+
 def test_cli_print_params_tau(cli, oracle):
     # -print-prms takes -t1/-t2 in every build (main_vnlb.cpp:173-174)
     r = run(cli, "-i", "unused", "-print-prms", 1, "-sigma", 20, "-t1", 50, "-t2", 12.5)
