@@ -40,7 +40,7 @@ STATUS = {
 EXPORTS = [
     "bm4dof_initialize_params", "bm4dof_set_size_search_window", "bm4dof_set_size_patch",
     "bm4dof_set_n_similar_patches", "bm4dof_format_params", "bm4dof_print_params",
-    "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run",
+    "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run", "bm4dof_process",
     "bm4dof_get_groups", "bm4dof_last_timings", "bm4dof_search_groups_noalloc",
     "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_gain_samples",
     "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_params", "bm4dof_trainer_grad",
@@ -79,6 +79,18 @@ class Params(C.Structure):
 
 class VideoSize(C.Structure):
     _fields_ = [("width", C.c_uint), ("height", C.c_uint), ("frames", C.c_uint), ("channels", C.c_uint)]
+
+
+class Crop(C.Structure):
+    """bm4dof_crop: the fields of VideoUtils::CropPosition that processNlBayes reads."""
+    _fields_ = [("origin_x", C.c_int), ("origin_y", C.c_int), ("origin_t", C.c_int),
+                ("ending_x", C.c_int), ("ending_y", C.c_int), ("ending_t", C.c_int),
+                ("source_sz", VideoSize)]
+
+
+def make_crop(origin, ending, source):
+    """origin/ending (x, y, t); source (width, height, frames, channels)."""
+    return Crop(*origin, *ending, VideoSize(*source))
 
 
 class Sequence(C.Structure):
@@ -138,6 +150,10 @@ def load(path: str = LIB_PATH):
                              C.c_uint, C.c_void_p, C.c_void_p, C.POINTER(Params), C.POINTER(Params),
                              C.c_uint, C.c_uint, C.POINTER(C.c_float)]
     L.bm4dof_run.restype = C.c_int
+    L.bm4dof_process.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint, C.c_uint, C.c_uint,
+                                 C.c_uint, C.c_void_p, C.c_void_p, C.POINTER(Params), C.POINTER(Crop), C.c_uint,
+                                 C.POINTER(C.c_uint)]
+    L.bm4dof_process.restype = C.c_int
     L.bm4dof_get_groups.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.POINTER(C.c_uint), C.POINTER(C.c_uint),
                                     C.POINTER(C.c_uint), C.c_uint, C.c_size_t, C.POINTER(C.c_size_t)]
     L.bm4dof_get_groups.restype = C.c_int
@@ -420,6 +436,26 @@ class Context:
             break
         keep = valid[: n.value].bool()
         return feat[: n.value][keep], tgt[: n.value][keep]
+
+    def processNlBayes(self, noisy, fflow, bflow, params, crop=None, basic=None, mixed=False, vbm3d=False,
+                       keep_groups=False):
+        """VideoNLB::processNlBayes: the step params.isFirstStep names, over one
+        video (numpy (F, C, H, W)) cut from a source as crop (make_crop) says.
+        Step 2 reads basic.  Returns (basic, final, groups)."""
+        flags = (KEEP_GROUPS if keep_groups else 0) | (MIXED_PRECISION if mixed else 0)
+        flags |= VBM3D_SEARCH if vbm3d else 0
+        noisy = np.ascontiguousarray(noisy, np.float32)
+        F, Cc, H, W = noisy.shape
+        ff = None if fflow is None else np.ascontiguousarray(fflow, np.float32)
+        bf = None if bflow is None else np.ascontiguousarray(bflow, np.float32)
+        b = np.zeros_like(noisy) if basic is None else np.array(basic, np.float32, copy=True)
+        fin = np.zeros_like(noisy)
+        ptr = lambda a: None if a is None else C.c_void_p(a.ctypes.data)
+        groups = C.c_uint()
+        _check(load().bm4dof_process(self._h, ptr(noisy), ptr(ff), ptr(bf), W, H, Cc, F, ptr(b), ptr(fin),
+                                     C.byref(params), None if crop is None else C.byref(crop), flags,
+                                     C.byref(groups)))
+        return b, fin, groups.value
 
     @staticmethod
     def tvl1_params(**kw):

@@ -159,11 +159,14 @@ struct Plan {
 };
 
 // Tiles (subDivideTight, lib_videot.hpp:853-916) and their reference grids
-// (processNlBayes, nldct.cpp:520-553).
-void make_plan(Plan &pl, unsigned W, unsigned H, unsigned F, unsigned nparts, const bm4dof_params &p)
+// (processNlBayes, nldct.cpp:520-553).  With borders (bm4dof_process) the plan
+// is one tile over the whole video whose sides {x0, y0, t0, x1, y1, t1} are
+// borders as given; the tiles of a run span all frames and have none in time.
+void make_plan(Plan &pl, unsigned W, unsigned H, unsigned F, unsigned nparts, const bm4dof_params &p,
+               const int *borders)
 {
-	unsigned a, b;
-	determine_factor(nparts, a, b);
+	unsigned a = 1, b = 1;
+	if (!borders) determine_factor(nparts, a, b);
 	pl.nW = (int)a;
 	pl.nH = (int)b;
 	pl.wTmp = (int)std::ceil(float(W) / float(pl.nW));
@@ -180,22 +183,34 @@ void make_plan(Plan &pl, unsigned W, unsigned H, unsigned F, unsigned nparts, co
 		for (int q = 0; q < pl.nW; q++) {
 			Tile T;
 			std::memset(&T, 0, sizeof(T));
-			T.ox = std::max(0, q * pl.wTmp - N);
-			T.oy = std::max(0, pp * pl.hTmp - N);
-			const int ex = std::min((int)W, (q + 1) * pl.wTmp + N);
-			const int ey = std::min((int)H, (pp + 1) * pl.hTmp + N);
-			T.w = ex - T.ox;
-			T.h = ey - T.oy;
-			T.bx0 = T.ox > 0;
-			T.by0 = T.oy > 0;
-			T.bx1 = ex < (int)W;
-			T.by1 = ey < (int)H;
+			bool bt0 = false, bt1 = false;
+			if (borders) {
+				T.w = (int)W;
+				T.h = (int)H;
+				T.bx0 = borders[0] != 0;
+				T.by0 = borders[1] != 0;
+				bt0 = borders[2] != 0;
+				T.bx1 = borders[3] != 0;
+				T.by1 = borders[4] != 0;
+				bt1 = borders[5] != 0;
+			} else {
+				T.ox = std::max(0, q * pl.wTmp - N);
+				T.oy = std::max(0, pp * pl.hTmp - N);
+				const int ex = std::min((int)W, (q + 1) * pl.wTmp + N);
+				const int ey = std::min((int)H, (pp + 1) * pl.hTmp + N);
+				T.w = ex - T.ox;
+				T.h = ey - T.oy;
+				T.bx0 = T.ox > 0;
+				T.by0 = T.oy > 0;
+				T.bx1 = ex < (int)W;
+				T.by1 = ey < (int)H;
+			}
 			const int ori_x = T.bx0 ? sPx - 1 + sWx / 2 : 0;
 			const int ori_y = T.by0 ? sPx - 1 + sWx / 2 : 0;
+			const int ori_f = bt0 ? sPt - 1 + sWt / 2 : 0;
 			const int end_x = T.w - (T.bx1 ? sPx - 1 + sWx / 2 : sPx - 1);
 			const int end_y = T.h - (T.by1 ? sPx - 1 + sWx / 2 : sPx - 1);
-			const int end_f = (int)F - (sPt - 1);   // tiles span all frames
-			(void)sWt;
+			const int end_f = (int)F - (bt1 ? sPt - 1 + sWt / 2 : sPt - 1);
 			std::vector<int> xs, ys, fs;
 			for (int x = ori_x, d = 0; x < end_x; x++, d++)
 				if ((unsigned)d % p.offSet == 0 || (!T.bx1 && x == end_x - 1) || (!T.bx0 && x == ori_x))
@@ -203,8 +218,8 @@ void make_plan(Plan &pl, unsigned W, unsigned H, unsigned F, unsigned nparts, co
 			for (int y = ori_y, d = 0; y < end_y; y++, d++)
 				if ((unsigned)d % p.offSet == 0 || (!T.by1 && y == end_y - 1) || (!T.by0 && y == ori_y))
 					ys.push_back(y);
-			for (int f = 0, d = 0; f < end_f; f++, d++)
-				if ((unsigned)d % p.offSetTime == 0 || f == end_f - 1) fs.push_back(f);
+			for (int f = ori_f, d = 0; f < end_f; f++, d++)
+				if ((unsigned)d % p.offSetTime == 0 || (!bt1 && f == end_f - 1)) fs.push_back(f);
 			T.nx = (int)xs.size();
 			T.ny = (int)ys.size();
 			T.nf = (int)fs.size();
@@ -276,6 +291,7 @@ struct RunMode {
 	bool vbm3d = false;     // predictive search of the reference's VBM3D_SEARCH build
 	float beta1 = 3.f;      // learned form: hard threshold of the non-mean rows
 	const SampleOut *samples = nullptr;   // training pairs instead of filtering
+	const int *borders = nullptr;         // bm4dof_process: one tile with these borders
 };
 
 // Host staging of one step's tables (pinned, so that the uploads are
@@ -388,7 +404,7 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	S.step = step;
 	S.p = p;
 	S.mode = mode;
-	make_plan(S.pl, W, H, F, nparts, p);
+	make_plan(S.pl, W, H, F, nparts, p, mode.borders);
 	const Plan &pl = S.pl;
 	StepParams &sp = S.sp;
 	std::memset(&sp, 0, sizeof(sp));
@@ -1087,6 +1103,70 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
 	CK(cudaStreamSynchronize(ctx->st));
 	collect_times(ctx);
 	return finish_run(ctx, r, ratios);
+}
+
+bm4dof_status bm4dof_process(bm4dof_ctx *ctx, const float *noisy, const float *fflow, const float *bflow,
+                             unsigned W, unsigned H, unsigned C, unsigned F, float *basic, float *final_,
+                             const bm4dof_params *params, const bm4dof_crop *crop, unsigned flags,
+                             unsigned *groups)
+{
+	clear_error();
+	if (!ctx || !params) {
+		set_error("bm4dof_process: null pointer or empty video");
+		return BM4DOF_ERR_ARGUMENT;
+	}
+	if (flags & BM4DOF_LEARNED) {
+		set_error("bm4dof_process: the learned form runs both steps (use bm4dof_run)");
+		return BM4DOF_ERR_UNSUPPORTED;
+	}
+	// processNlBayes runs the step that isFirstStep names (nldct.cpp:502, 740)
+	const bool step1 = params->isFirstStep != 0;
+	RunArgs r;
+	r.noisy = noisy;
+	r.fflow = fflow;
+	r.bflow = bflow;
+	r.W = W;
+	r.H = H;
+	r.C = C;
+	r.F = F;
+	r.basic = basic;
+	r.final_ = final_;
+	r.p1 = *params;
+	r.p2 = *params;
+	(step1 ? r.p2 : r.p1).sizePatch = 0;
+	r.nparts = 1;
+	r.flags = flags;
+	bm4dof_status e = validate_run(r, "bm4dof_process");
+	if (e != BM4DOF_OK) return e;
+	// the crop's sides that stop short of its source (nldct.cpp:520-525)
+	int borders[6] = {0, 0, 0, 0, 0, 0};
+	if (crop) {
+		borders[0] = crop->origin_x > 0;
+		borders[1] = crop->origin_y > 0;
+		borders[2] = crop->origin_t > 0;
+		borders[3] = crop->ending_x < (int)crop->source_sz.width;
+		borders[4] = crop->ending_y < (int)crop->source_sz.height;
+		borders[5] = crop->ending_t < (int)crop->source_sz.frames;
+	}
+	r.mode.borders = borders;
+	r.yuv1 = r.yuv2 = false;   // no colour transform of its own
+	CK(cudaSetDevice(ctx->device));
+	begin_call(ctx);
+	if (!ctx->t_begin) {
+		CK(cudaEventCreate(&ctx->t_begin));
+		CK(cudaEventCreate(&ctx->t_end));
+	}
+	set_budget(ctx);
+	ctx->whf = (float)(W * H * F);
+	if ((e = prepare_run(ctx, r)) != BM4DOF_OK) return e;
+	CK(cudaEventRecord(ctx->t_begin, ctx->st));
+	if ((e = launch_run(ctx, r)) != BM4DOF_OK) return e;
+	CK(cudaEventRecord(ctx->t_end, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	collect_times(ctx);
+	if ((e = finish_run(ctx, r, nullptr)) != BM4DOF_OK) return e;
+	if (groups) *groups = ext(ctx).steps[step1 ? 0 : 1].h_small[64];
+	return BM4DOF_OK;
 }
 
 }  // extern "C"

@@ -157,6 +157,33 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx,
                          const bm4dof_params *params1, const bm4dof_params *params2,
                          unsigned nparts, unsigned flags, float ratios[2]);
 
+/* The fields of VideoUtils::CropPosition (src/utils/lib_videot.hpp:440-470)
+ * that processNlBayes reads: where the processed video was cut from its
+ * source.  All zero (the reference's default CropPosition()) means no border. */
+typedef struct bm4dof_crop {
+	int origin_x, origin_y, origin_t;   /* first column, row and frame of the crop */
+	int ending_x, ending_y, ending_t;   /* one past the last                       */
+	bm4dof_video_size source_sz;        /* size of the video it was cut from       */
+} bm4dof_crop;
+
+/* VideoNLB::processNlBayes, src/core/nldct.cpp:490-890: one step
+ * (params->isFirstStep) over one video, typically a tile cut from a larger
+ * one, with no tiling and no colour transform of its own.  Reference patches
+ * are taken on the grid of nldct.cpp:520-553: on a side where the crop does
+ * not reach the source's edge (origin > 0, or ending < the source size), the
+ * grid keeps sizePatch-1 + sizeSearchWindow/2 pixels (sizePatchTime-1 +
+ * (range)/2 frames) away from it.  Step 1 writes basic, step 2 reads basic and
+ * writes final; both aggregate over the whole video (pixels no patch covers
+ * are divided by the noisy value, as nldct.cpp:2436-2448 does).
+ *  crop    NULL for no border.
+ *  groups  out: the number of processed groups (the reference's return value).
+ * Flags as bm4dof_run; BM4DOF_LEARNED is rejected (it needs both steps). */
+bm4dof_status bm4dof_process(bm4dof_ctx *ctx,
+                             const float *noisy, const float *fflow, const float *bflow,
+                             unsigned width, unsigned height, unsigned channels, unsigned frames,
+                             float *basic, float *final_, const bm4dof_params *params,
+                             const bm4dof_crop *crop, unsigned flags, unsigned *groups);
+
 /* Neighbour lists of the last bm4dof_run made with BM4DOF_KEEP_GROUPS, for one
  * step (1 or 2) and tile.  For each processed group in processing order:
  *   ref[g]          reference patch index (tile video index at channel 0, as

@@ -3,7 +3,8 @@
  * For code written against namespace VideoNLB (src/core/nldct.h): runNlBayes
  * with the reference's parameters and return value (nldct.h:239-247) and its
  * error behaviour (std::runtime_error carrying the messages of
- * nldct.cpp:279-341, which the C ABI keeps verbatim), and the parameter
+ * nldct.cpp:279-341, which the C ABI keeps verbatim), processNlBayes for one
+ * step over one cropped video (nldct.h:270-278), and the parameter
  * functions initializeNlbParameters, setSizeSearchWindow, setSizePatch,
  * setNSimilarPatches and printNlbParameters (nldct.h:149-224).
  * Header-only; link -lbm4dof_gpu.
@@ -13,7 +14,9 @@
  *   Params  any struct with nlbParams' fields, by name (nldct.h:55-82);
  *   Size    any struct with VideoSize's width, height, frames, channels;
  *   Video   any type with Video<float>'s members sz (a Size), data (contiguous
- *           float storage with data()) and resize(const Size &).
+ *           float storage with data()) and resize(const Size &);
+ *   Crop    any struct with VideoUtils::CropPosition's origin_x/y/t,
+ *           ending_x/y/t and source_sz (lib_videot.hpp:440-470).
  * A reference build switches by calling bm4dof_videonlb::runNlBayes where it
  * called VideoNLB::runNlBayes; everything else stays as it is.
  *
@@ -241,6 +244,60 @@ std::vector<float> runNlBayes(Video const &noisy, Video const &fflow, Video cons
 	               flags, ratios);
 	if (s != BM4DOF_OK) throw std::runtime_error(bm4dof_last_error());
 	return {ratios[0], ratios[1]};
+}
+
+/* VideoNLB::processNlBayes (nldct.cpp:490-890) on the GPU: the step that
+ * p.isFirstStep names, over one video cut from a source as crop says; step 1
+ * writes basic, step 2 reads it and writes final (each resized to the video,
+ * as the reference does).  Returns the number of processed groups.  The
+ * reference checks nothing here; the layer refuses flows or a step-2 basic
+ * whose size differs from the video's, which the reference would read past. */
+template <class Video, class Params, class Crop>
+unsigned processNlBayes(Video const &noisy, Video const &fflow, Video const &bflow, Video &basic, Video &final,
+                        Params const &p, Crop const &crop, unsigned flags = 0, int device = 0)
+{
+	const bool use_oflow = fflow.sz.width > 0;
+	const auto flow_ok = [&noisy](const Video &f) {
+		return f.sz.channels == 2 && f.sz.width == noisy.sz.width && f.sz.height == noisy.sz.height &&
+		       f.sz.frames == noisy.sz.frames;
+	};
+	if (use_oflow && (!flow_ok(fflow) || !flow_ok(bflow)))
+		throw std::runtime_error("bm4dof_process: the flows' size differs from the video's");
+	if (p.isFirstStep) basic.resize(noisy.sz);
+	else if (!detail::same_size(noisy.sz, basic.sz))
+		throw std::runtime_error("bm4dof_process: the basic estimate's size differs from the video's");
+	else final.resize(noisy.sz);
+	bm4dof_crop c;
+	c.origin_x = crop.origin_x;
+	c.origin_y = crop.origin_y;
+	c.origin_t = crop.origin_t;
+	c.ending_x = crop.ending_x;
+	c.ending_y = crop.ending_y;
+	c.ending_t = crop.ending_t;
+	c.source_sz = to_c_size(crop.source_sz);
+	bm4dof_ctx *ctx = detail::context(device);
+	const bm4dof_params cp = to_c(p);
+	unsigned groups = 0;
+	const bm4dof_status s = bm4dof_process(
+	    ctx, noisy.data.data(), use_oflow ? fflow.data.data() : nullptr, use_oflow ? bflow.data.data() : nullptr,
+	    noisy.sz.width, noisy.sz.height, noisy.sz.channels, noisy.sz.frames, basic.data.data(),
+	    p.isFirstStep ? nullptr : final.data.data(), &cp, &c, flags, &groups);
+	if (s != BM4DOF_OK) throw std::runtime_error(bm4dof_last_error());
+	return groups;
+}
+
+/* processNlBayes with the reference's default crop (no border). */
+template <class Video, class Params>
+unsigned processNlBayes(Video const &noisy, Video const &fflow, Video const &bflow, Video &basic, Video &final,
+                        Params const &p)
+{
+	struct NoCrop {
+		int origin_x = 0, origin_y = 0, origin_t = 0, ending_x = 0, ending_y = 0, ending_t = 0;
+		struct {
+			unsigned width = 0, height = 0, frames = 0, channels = 0;
+		} source_sz;
+	};
+	return processNlBayes(noisy, fflow, bflow, basic, final, p, NoCrop());
 }
 
 /* The reference's own signature: tiles from default_tiles(). */

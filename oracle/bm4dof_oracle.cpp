@@ -182,6 +182,7 @@ void determine_factor(unsigned n, unsigned &a, unsigned &b)
 struct Crop {
 	int ox, oy, ex, ey;   /* crop box [ox,ex) x [oy,ey), all frames */
 	bool bx0, by0, bx1, by1;
+	bool bt0 = false, bt1 = false;   /* temporal borders: processNlBayes alone */
 };
 
 void tile_grid(unsigned W, unsigned H, unsigned nparts, int &nW, int &nH, int &wTmp, int &hTmp)
@@ -861,9 +862,10 @@ unsigned process_tile(const Vid &noisy, const Vid &fflow, const Vid &bflow, Vid 
 	Vid weight(W, H, F, 1, 0.f);
 	std::vector<char> mask((size_t)W * H * F, 0);
 
-	/* reference-patch grid, nldct.cpp:520-553 (tiles always span all frames) */
-	const bool bx0 = crop.bx0, by0 = crop.by0, bt0 = false;
-	const bool bx1 = crop.bx1, by1 = crop.by1, bt1 = false;
+	/* reference-patch grid, nldct.cpp:520-553 (the tiles of a run span all
+	 * frames: temporal borders come only from a caller's crop) */
+	const bool bx0 = crop.bx0, by0 = crop.by0, bt0 = crop.bt0;
+	const bool bx1 = crop.bx1, by1 = crop.by1, bt1 = crop.bt1;
 	const int ori_x = bx0 ? sPx - 1 + sWx / 2 : 0;
 	const int ori_y = by0 ? sPx - 1 + sWx / 2 : 0;
 	const int ori_f = bt0 ? sPt - 1 + sWt / 2 : 0;
@@ -1176,6 +1178,51 @@ int oracle_run_ex(const float *noisy_in, const float *fflow_in, const float *bfl
 				}
 		trace->count = k;
 	}
+	return 0;
+}
+
+/* VideoNLB::processNlBayes (nldct.cpp:490-890): one step (p->isFirstStep) of
+ * one video with the border flags of its crop (nldct.cpp:520-525; crop may be
+ * NULL), no tiling, no colour transform.  Step 1 writes basic_io, step 2 reads
+ * it and writes final_out.  Returns the processed group count in *groups. */
+int oracle_process(const float *noisy_in, const float *fflow_in, const float *bflow_in,
+                   unsigned W, unsigned H, unsigned C, unsigned F, float *basic_io, float *final_out,
+                   const bm4dof_params *p, const bm4dof_crop *crop, unsigned flags, unsigned *groups,
+                   char *err, size_t errlen)
+{
+	if (p->transform == BM4DOF_BIOR1_5 && p->sizePatch != 8)
+		return fail(err, errlen, "VideoNLB::processNlBayes: bior1_5 transform is only implemented for patches of size 8 x 8 x pt.", BM4DOF_ERR_BIOR_SIZE);
+	if (p->sizePatch == 0 || p->offSet == 0 || p->offSetTime == 0 || p->sizePatchTime == 0)
+		return fail(err, errlen, "oracle: unsupported parameters", BM4DOF_ERR_UNSUPPORTED);
+	Crop c;
+	c.ox = c.oy = 0;
+	c.ex = (int)W;
+	c.ey = (int)H;
+	c.bx0 = c.by0 = c.bx1 = c.by1 = false;
+	if (crop) {
+		c.bx0 = crop->origin_x > 0;
+		c.by0 = crop->origin_y > 0;
+		c.bt0 = crop->origin_t > 0;
+		c.bx1 = crop->ending_x < (int)crop->source_sz.width;
+		c.by1 = crop->ending_y < (int)crop->source_sz.height;
+		c.bt1 = crop->ending_t < (int)crop->source_sz.frames;
+	}
+	Vid noisy(W, H, F, C);
+	std::copy(noisy_in, noisy_in + noisy.d.size(), noisy.d.begin());
+	Vid fflow, bflow;
+	if (fflow_in) {
+		fflow = Vid(W, H, F, 2);
+		bflow = Vid(W, H, F, 2);
+		std::copy(fflow_in, fflow_in + fflow.d.size(), fflow.d.begin());
+		std::copy(bflow_in, bflow_in + bflow.d.size(), bflow.d.begin());
+	}
+	Vid basic(W, H, F, C), out;
+	if (!p->isFirstStep) std::copy(basic_io, basic_io + basic.d.size(), basic.d.begin());
+	const unsigned n = process_tile(noisy, fflow, bflow, basic, out, *p, c, nullptr,
+	                                (flags & BM4DOF_VBM3D_SEARCH) != 0);
+	if (p->isFirstStep) std::copy(basic.d.begin(), basic.d.end(), basic_io);
+	else std::copy(out.d.begin(), out.d.end(), final_out);
+	if (groups) *groups = n;
 	return 0;
 }
 

@@ -43,6 +43,37 @@ class VideoSize(C.Structure):
     _fields_ = [("width", C.c_uint), ("height", C.c_uint), ("frames", C.c_uint), ("channels", C.c_uint)]
 
 
+class Crop(C.Structure):
+    """Layout of bm4dof_crop (include/bm4dof.h): the fields of
+    VideoUtils::CropPosition that processNlBayes reads."""
+    _fields_ = [("origin_x", C.c_int), ("origin_y", C.c_int), ("origin_t", C.c_int),
+                ("ending_x", C.c_int), ("ending_y", C.c_int), ("ending_t", C.c_int),
+                ("source_sz", VideoSize)]
+
+
+def make_crop(origin, ending, source):
+    """origin/ending (x, y, t), source (width, height, frames, channels)."""
+    return Crop(*origin, *ending, VideoSize(*source))
+
+
+def _process(fn, noisy, fflow, bflow, prm, crop, basic, *extra):
+    """Shared by Oracle.processNlBayes and Reference.processNlBayes: one step of
+    processNlBayes; returns (basic, final, groups)."""
+    noisy = np.ascontiguousarray(noisy, np.float32)
+    F, Cc, H, W = noisy.shape
+    fflow = None if fflow is None else np.ascontiguousarray(fflow, np.float32)
+    bflow = None if bflow is None else np.ascontiguousarray(bflow, np.float32)
+    b = np.zeros_like(noisy) if basic is None else np.array(basic, np.float32, copy=True)
+    fin = np.zeros_like(noisy)
+    groups = C.c_uint()
+    err = C.create_string_buffer(512)
+    rc = fn(_fp(noisy), _fp(fflow), _fp(bflow), W, H, Cc, F, _fp(b), _fp(fin), C.byref(prm),
+            None if crop is None else C.byref(crop), *extra, C.byref(groups), err, 512)
+    if rc:
+        raise RuntimeError(err.value.decode())
+    return b, fin, groups.value
+
+
 class Trace(C.Structure):
     _fields_ = [("cap", C.c_uint), ("stride", C.c_uint),
                 ("step", C.POINTER(C.c_uint)), ("tile", C.POINTER(C.c_uint)),
@@ -121,6 +152,15 @@ class Oracle(_Lib):
         L.oracle_tile_crops.restype = C.c_int
         L.oracle_determine_factor.argtypes = [C.c_uint, C.POINTER(C.c_uint), C.POINTER(C.c_uint)]
         L.oracle_color_transform.argtypes = [C.POINTER(C.c_float), C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_int]
+        L.oracle_process.restype = C.c_int
+        L.oracle_process.argtypes = [C.POINTER(C.c_float)] * 3 + [C.c_uint] * 4 + [C.POINTER(C.c_float)] * 2 + \
+            [C.POINTER(Params), C.POINTER(Crop), C.c_uint, C.POINTER(C.c_uint), C.c_char_p, C.c_size_t]
+
+    def processNlBayes(self, noisy, fflow, bflow, prm, crop=None, basic=None, vbm3d=False):
+        """VideoNLB::processNlBayes: the step prm.isFirstStep names, over one
+        video cut from a source as crop says.  Returns (basic, final, groups)."""
+        return _process(self.lib.oracle_process, noisy, fflow, bflow, prm, crop, basic,
+                        VBM3D_SEARCH if vbm3d else 0)
 
     def runNlBayes(self, noisy, fflow, bflow, p1, p2, basic=None, nparts=2, nthreads=1,
                    trace_cap=0, trace_stride=16, vbm3d=False):
@@ -199,6 +239,13 @@ class Reference(_Lib):
         L.ref_search.restype = C.c_uint
         L.ref_search.argtypes = [C.c_uint] + [C.POINTER(C.c_float)] * 4 + [C.c_uint] * 4 + \
             [C.POINTER(Params), C.c_uint, C.POINTER(C.c_uint)]
+        L.ref_process.restype = C.c_int
+        L.ref_process.argtypes = [C.POINTER(C.c_float)] * 3 + [C.c_uint] * 4 + [C.POINTER(C.c_float)] * 2 + \
+            [C.POINTER(Params), C.POINTER(Crop), C.POINTER(C.c_uint), C.c_char_p, C.c_size_t]
+
+    def processNlBayes(self, noisy, fflow, bflow, prm, crop=None, basic=None):
+        """The reference's own VideoNLB::processNlBayes.  Returns (basic, final, groups)."""
+        return _process(self.lib.ref_process, noisy, fflow, bflow, prm, crop, basic)
 
     @staticmethod
     def available(path=REF_SO):

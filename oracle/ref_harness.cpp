@@ -177,6 +177,47 @@ int ref_run(const float *noisy, const float *fflow, const float *bflow, unsigned
 	}
 }
 
+/* processNlBayes (nldct.cpp:490) of one video with the crop position given
+ * (NULL: the default CropPosition()).  Step 1 writes basic, step 2 reads it
+ * and writes final_.  Returns 0 with the group count in *groups, or 1 with the
+ * exception text in err. */
+int ref_process(const float *noisy, const float *fflow, const float *bflow, unsigned W, unsigned H,
+                unsigned C, unsigned F, float *basic, float *final_, const bm4dof_params *p,
+                const bm4dof_crop *crop, unsigned *groups, char *err, size_t errlen)
+{
+	try {
+		Video<float> vn, vf, vb, vbasic, vfinal;
+		fill(vn, noisy, W, H, F, C);
+		if (fflow) fill(vf, fflow, W, H, F, 2);
+		if (bflow) fill(vb, bflow, W, H, F, 2);
+		VideoNLB::nlbParams q;
+		to_nlb(*p, q);
+		if (!q.isFirstStep) fill(vbasic, basic, W, H, F, C);
+		VideoUtils::CropPosition cp = VideoUtils::CropPosition();
+		if (crop) {
+			cp.origin_x = crop->origin_x;
+			cp.origin_y = crop->origin_y;
+			cp.origin_t = crop->origin_t;
+			cp.ending_x = crop->ending_x;
+			cp.ending_y = crop->ending_y;
+			cp.ending_t = crop->ending_t;
+			cp.source_sz = VideoSize(crop->source_sz.width, crop->source_sz.height, crop->source_sz.frames,
+			                         crop->source_sz.channels);
+		}
+		const unsigned n = VideoNLB::processNlBayes(vn, vf, vb, vbasic, vfinal, q, cp);
+		const size_t nv = (size_t)W * H * F * C;
+		if (q.isFirstStep && vbasic.data.size() == nv)
+			std::memcpy(basic, vbasic.data.data(), sizeof(float) * nv);
+		if (!q.isFirstStep && vfinal.data.size() == nv)
+			std::memcpy(final_, vfinal.data.data(), sizeof(float) * nv);
+		if (groups) *groups = n;
+		return 0;
+	} catch (const std::exception &e) {
+		if (err && errlen) std::snprintf(err, errlen, "%s", e.what());
+		return 1;
+	}
+}
+
 /* estimateSimilarPatchesStep1/2 (nldct.cpp:1143, 1607) on one video (a tile):
  * returns nSimP and writes index[0..nSimP). */
 unsigned ref_search(unsigned step, const float *noisy, const float *basic, const float *fflow,

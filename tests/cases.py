@@ -44,3 +44,21 @@ VBM3D_CASES = [
     ("vbm3d_image", 48, 40, 1, 1, 20.0, 37, False, CFG_IMAGE, 1),
     ("vbm3d_paste", 40, 36, 6, 1, 20.0, 38, True, dict(CFG_VIDEO, paste_boost=True), 1),
 ]
+
+# VideoNLB::processNlBayes on one video cut from a larger source: each case is
+# (name, W, H, F, C, sigma, seed, flow, cli-params, temporal range or None,
+# crop ((origin x, y, t), (ending x, y, t), (source W, H, F, C)) or None,
+# vbm3d).  Step 1 is run on the crop, then step 2 on the crop with that basic.
+PROCESS_CASES = [
+    ("process_image", 40, 36, 1, 1, 20.0, 41, False, CFG_IMAGE, None, None, False),
+    ("process_left", 40, 36, 6, 1, 20.0, 42, True, CFG_VIDEO, None, ((12, 0, 0), (52, 36, 6), (52, 36, 6, 1)), False),
+    ("process_inner", 40, 36, 6, 1, 20.0, 43, True, CFG_VIDEO, None, ((10, 8, 0), (50, 44, 6), (70, 60, 6, 1)), False),
+    ("process_time", 32, 28, 12, 1, 20.0, 44, True, CFG_VIDEO, 1, ((0, 0, 2), (32, 28, 14), (32, 28, 17, 1)), False),
+    ("process_rgb_right", 30, 28, 4, 3, 20.0, 45, True, CFG_VIDEO, None, ((0, 0, 0), (30, 28, 4), (60, 28, 4, 3)), False),
+    ("process_paste_top", 40, 36, 6, 1, 20.0, 46, True, dict(CFG_VIDEO, paste_boost=True), None,
+     ((0, 6, 0), (40, 42, 6), (40, 42, 6, 1)), False),
+    ("process_noflow_bottom", 36, 32, 5, 1, 20.0, 47, False, CFG_VIDEO, None, ((0, 0, 0), (36, 32, 5), (36, 50, 5, 1)),
+     False),
+    ("process_vbm3d_inner", 40, 36, 6, 1, 20.0, 48, True, CFG_VIDEO, None, ((4, 4, 0), (44, 40, 6), (60, 50, 6, 1)),
+     True),
+]

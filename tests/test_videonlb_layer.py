@@ -127,3 +127,34 @@ def test_gpu_layer_run_equals_the_library(layer, gpulib, gpuctx, tmp_path):
     b, f, ratios = gpuctx.runNlBayes(noisy, None, None, p1, p2, nparts=4)
     assert np.array_equal(basic, b) and np.array_equal(final, f)
     assert [float(x) for x in r.stdout.split()] == pytest.approx([float(x) for x in ratios], abs=1e-5)
+
+
+def test_layer_process_refuses_sizes_it_cannot_read(layer):
+    r = run(layer, "process_errors")
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.splitlines() == [
+        "flows: bm4dof_process: the flows' size differs from the video's",
+        "basic: bm4dof_process: the basic estimate's size differs from the video's",
+    ]
+
+
+@pytest.mark.gpu
+def test_gpu_layer_process_equals_the_library(layer, gpulib, gpuctx, tmp_path):
+    W, H, F, sigma = 40, 36, 4, 20.0
+    clean, nz, _, _ = video_case(W, H, F, sigma=sigma, seed=27)
+    noisy = np.ascontiguousarray(nz, np.float32)
+    noisy.tofile(tmp_path / "n.raw")
+    crop = ((6, 0, 0), (46, 36, 4), (60, 50, 4))    # borders on the left, the right and the bottom
+    r = run(layer, "process", W, H, 1, F, sigma, tmp_path / "n.raw", tmp_path / "b.raw", tmp_path / "f.raw",
+            *crop[0], *crop[1], *crop[2])
+    assert r.returncode == 0, r.stderr
+    basic = np.fromfile(tmp_path / "b.raw", np.float32).reshape(noisy.shape)
+    final = np.fromfile(tmp_path / "f.raw", np.float32).reshape(noisy.shape)
+    size = (W, H, F, 1)
+    p1 = gpulib.initializeNlbParameters(1, sigma, size)
+    p2 = gpulib.initializeNlbParameters(2, sigma, size)
+    c = gpulib.make_crop(crop[0], crop[1], (*crop[2], 1))
+    b, _, g1 = gpuctx.processNlBayes(noisy, None, None, p1, c)
+    _, f, g2 = gpuctx.processNlBayes(noisy, None, None, p2, c, basic=b)
+    assert np.array_equal(basic, b) and np.array_equal(final, f)
+    assert [int(x) for x in r.stdout.split()] == [g1, g2]

@@ -9,8 +9,13 @@
 //   videonlb_layer params      parameters resolved through the layer, printed
 //   videonlb_layer roundtrip   field-for-field conversion both ways
 //   videonlb_layer errors      runNlBayes on inputs the reference rejects
+//   videonlb_layer process_errors   processNlBayes on inputs the layer refuses
 //   videonlb_layer run W H C F sigma nparts noisy.raw basic.raw final.raw
 //                              one denoising run (needs a GPU), planar floats
+//   videonlb_layer process W H C F sigma noisy.raw basic.raw final.raw
+//                  ox oy ot ex ey et sw sh sf
+//                              processNlBayes step 1 then step 2 on one crop
+//                              (needs a GPU); prints the two group counts
 #include <ctime>
 #include <cstdio>
 #include <cstdlib>
@@ -216,6 +221,26 @@ int cmd_errors()
 	return bad ? 1 : 0;
 }
 
+struct CropArgs {
+	int origin_x, origin_y, origin_t, ending_x, ending_y, ending_t;
+	Size source_sz;
+};
+
+int cmd_process_errors()
+{
+	const Size sz(16, 12, 3, 1);
+	Params p1 = Params(), p2 = Params();
+	L::initializeNlbParameters(p1, 1, 20.f, sz, false);
+	L::initializeNlbParameters(p2, 2, 20.f, sz, false);
+	const Vid noisy(sz), bad_flow(Size(16, 12, 2, 2)), flow(Size(16, 12, 3, 2)), empty;
+	Vid basic, fin, small_basic(Size(16, 12, 2, 1));
+	std::printf("flows: %s\n", message([&] { L::processNlBayes(noisy, bad_flow, flow, basic, fin, p1); }).c_str());
+	std::printf("basic: %s\n",
+	            message([&] { L::processNlBayes(noisy, empty, empty, small_basic, fin, p2); }).c_str());
+	std::fflush(stdout);
+	return 0;
+}
+
 bool read_raw(const char *path, std::vector<float> &v)
 {
 	FILE *f = std::fopen(path, "rb");
@@ -254,6 +279,32 @@ int cmd_run(char **a)
 	return write_raw(a[7], basic.data) && write_raw(a[8], fin.data) ? 0 : 1;
 }
 
+int cmd_process(char **a)
+{
+	const Size sz((unsigned)std::atoi(a[0]), (unsigned)std::atoi(a[1]), (unsigned)std::atoi(a[3]),
+	              (unsigned)std::atoi(a[2]));
+	const float sigma = (float)std::atof(a[4]);
+	CropArgs c;
+	int *f[6] = {&c.origin_x, &c.origin_y, &c.origin_t, &c.ending_x, &c.ending_y, &c.ending_t};
+	for (int k = 0; k < 6; k++) *f[k] = std::atoi(a[8 + k]);
+	c.source_sz = Size((unsigned)std::atoi(a[14]), (unsigned)std::atoi(a[15]), (unsigned)std::atoi(a[16]),
+	                   sz.channels);
+	Vid noisy(sz), basic, fin;
+	const Vid empty;
+	if (!read_raw(a[5], noisy.data)) return std::fprintf(stderr, "cannot read %s\n", a[5]), 1;
+	Params p1 = Params(), p2 = Params();
+	L::initializeNlbParameters(p1, 1, sigma, sz, false);
+	L::initializeNlbParameters(p2, 2, sigma, sz, false);
+	try {
+		const unsigned g1 = L::processNlBayes(noisy, empty, empty, basic, fin, p1, c);
+		const unsigned g2 = L::processNlBayes(noisy, empty, empty, basic, fin, p2, c);
+		std::printf("%u %u\n", g1, g2);
+	} catch (const std::exception &e) {
+		return std::fprintf(stderr, "%s\n", e.what()), 1;
+	}
+	return write_raw(a[6], basic.data) && write_raw(a[7], fin.data) ? 0 : 1;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -262,7 +313,9 @@ int main(int argc, char **argv)
 	if (c == "params") return cmd_params();
 	if (c == "roundtrip") return cmd_roundtrip();
 	if (c == "errors") return cmd_errors();
+	if (c == "process_errors") return cmd_process_errors();
 	if (c == "run" && argc == 11) return cmd_run(argv + 2);
-	std::fprintf(stderr, "usage: videonlb_layer params|roundtrip|errors|run ...\n");
+	if (c == "process" && argc == 19) return cmd_process(argv + 2);
+	std::fprintf(stderr, "usage: videonlb_layer params|roundtrip|errors|process_errors|run|process ...\n");
 	return 2;
 }
