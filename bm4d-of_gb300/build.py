@@ -22,6 +22,8 @@ LIB = os.path.join(OUT, "libbm4dof_gpu.so")
 CLI = os.path.join(OUT, "bm4dof")          # the command line, linked to LIB
 TVL1_CLI = os.path.join(OUT, "tvl1flow")   # the optical-flow command line, linked to LIB
 CLI_ALIAS = os.path.join(OUT, "bm4d-of")   # the name the reference's scripts call the CLI by
+AWGN_CLI = os.path.join(OUT, "awgn")       # noise and PSNR tools of the reference's scripts (host only)
+PSNR_CLI = os.path.join(OUT, "psnr")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
@@ -57,17 +59,18 @@ def _compile(src: str, verbose: bool) -> str:
     return obj
 
 
-def _link_cli(main_src: str, exe: str) -> None:
-    """A command line over LIB: main_src plus the frame files, host code only
-    (no contraction, so the double arithmetic of the colour reduction rounds
-    alike on every host)."""
+def _link_cli(main_src: str, exe: str, gpu: bool = True) -> None:
+    """A command line: main_src plus the frame files, host code only, linked
+    to LIB when gpu (no contraction, so that double arithmetic such as the
+    colour reduction rounds alike on every host)."""
     src = [os.path.join(SRC, main_src), os.path.join(SRC, "frames.cpp")]
-    deps = src + [os.path.join(SRC, "frames.hpp"), os.path.join(HERE, "..", "include", "bm4dof.h"), LIB]
+    deps = src + [os.path.join(SRC, "frames.hpp"), os.path.join(HERE, "..", "include", "bm4dof.h")]
+    deps += [LIB] if gpu else []
     if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(x) for x in deps):
         return
     cxx = shutil.which("g++") or "g++"
-    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", *src, "-o", exe, "-L" + OUT, "-lbm4dof_gpu",
-           "-Wl,-rpath,$ORIGIN"]
+    link = ["-L" + OUT, "-lbm4dof_gpu", "-Wl,-rpath,$ORIGIN"] if gpu else []
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", *src, "-o", exe, *link]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"{os.path.basename(exe)} build failed:\n{r.stdout}\n{r.stderr}")
@@ -82,8 +85,10 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
-        list(ex.map(lambda a: _link_cli(*a), [("cli.cpp", CLI), ("tvl1_cli.cpp", TVL1_CLI)]))
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:
+        list(ex.map(lambda a: _link_cli(*a), [("cli.cpp", CLI), ("tvl1_cli.cpp", TVL1_CLI),
+                                               ("awgn_cli.cpp", AWGN_CLI, False),
+                                               ("psnr_cli.cpp", PSNR_CLI, False)]))
     if not os.path.lexists(CLI_ALIAS):
         os.symlink(os.path.basename(CLI), CLI_ALIAS)
     return LIB

@@ -18,8 +18,9 @@
 #include "../../include/bm4dof.h"
 #include "frames.hpp"
 
-using bm4dof_frames::read_frame;
-using bm4dof_frames::write_frame;
+using bm4dof_frames::load_video;
+using bm4dof_frames::save_video;
+using bm4dof_frames::Video;
 
 namespace {
 
@@ -63,63 +64,6 @@ struct Args {
 		if (help) std::printf("    %-12s = %-16s : %s\n", n, d, use);
 	}
 };
-
-struct Video {
-	std::vector<float> data;
-	unsigned w = 0, h = 0, c = 0, f = 0;
-};
-
-// Video<float>::loadVideo (lib_videot.cpp:30-89)
-bool load_video(const std::string &pattern, unsigned first, unsigned last, unsigned step, Video &v,
-                std::string &err)
-{
-	char name[1024];
-	std::snprintf(name, sizeof name, pattern.c_str(), first);
-	std::vector<float> frame;
-	int w, h, c;
-	if (!read_frame(name, frame, w, h, c)) {
-		err = "Video<T>::loadVideo: loading of " + std::string(name) + " failed";
-		return false;
-	}
-	v.w = w;
-	v.h = h;
-	v.c = c;
-	v.f = (last - first + 1) / step;
-	v.data.assign((size_t)v.w * v.h * v.c * v.f, 0.f);
-	size_t o = 0;
-	std::copy(frame.begin(), frame.end(), v.data.begin());
-	o += frame.size();
-	for (unsigned t = first + step; t <= last; t += step) {
-		std::snprintf(name, sizeof name, pattern.c_str(), t);
-		if (!read_frame(name, frame, w, h, c)) {
-			err = "Video<T>::loadVideo: loading of " + std::string(name) + " failed";
-			return false;
-		}
-		if ((unsigned)w != v.w || (unsigned)h != v.h || (unsigned)c != v.c) {
-			err = "Video<T>::loadVideo: size of " + std::string(name) + " does not match video size";
-			return false;
-		}
-		if (o + frame.size() > v.data.size()) v.data.resize(o + frame.size());
-		std::copy(frame.begin(), frame.end(), v.data.begin() + o);
-		o += frame.size();
-	}
-	return true;
-}
-
-// Video<float>::saveVideo (lib_videot.cpp:91-126)
-bool save_video(const std::string &pattern, unsigned first, unsigned step, const Video &v, std::string &err)
-{
-	const size_t whc = (size_t)v.w * v.h * v.c;
-	for (unsigned k = 0; k < v.f; k++) {
-		char name[1024];
-		std::snprintf(name, sizeof name, pattern.c_str(), first + k * step);
-		if (!write_frame(name, v.data.data() + k * whc, v.w, v.h, v.c)) {
-			err = "Video<T>::saveVideo: writing of " + std::string(name) + " failed";
-			return false;
-		}
-	}
-	return true;
-}
 
 // printNlbParameters (nldct.cpp:212-248); the predictive search adds three
 // lines to the patch-search block, as the reference's VBM3D_SEARCH build does.

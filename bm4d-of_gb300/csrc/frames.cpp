@@ -378,6 +378,56 @@ bool read_frame(const char *path, std::vector<float> &out, int &w, int &h, int &
 	return ok;
 }
 
+bool load_video(const std::string &pattern, unsigned first, unsigned last, unsigned step, Video &v,
+                std::string &err)
+{
+	char name[1024];
+	std::snprintf(name, sizeof name, pattern.c_str(), first);
+	std::vector<float> frame;
+	int w, h, c;
+	if (!read_frame(name, frame, w, h, c)) {
+		err = "Video<T>::loadVideo: loading of " + std::string(name) + " failed";
+		return false;
+	}
+	v.w = w;
+	v.h = h;
+	v.c = c;
+	v.f = (last - first + 1) / step;
+	v.data.assign((size_t)v.w * v.h * v.c * v.f, 0.f);
+	size_t o = 0;
+	std::copy(frame.begin(), frame.end(), v.data.begin());
+	o += frame.size();
+	for (unsigned t = first + step; t <= last; t += step) {
+		std::snprintf(name, sizeof name, pattern.c_str(), t);
+		if (!read_frame(name, frame, w, h, c)) {
+			err = "Video<T>::loadVideo: loading of " + std::string(name) + " failed";
+			return false;
+		}
+		if ((unsigned)w != v.w || (unsigned)h != v.h || (unsigned)c != v.c) {
+			err = "Video<T>::loadVideo: size of " + std::string(name) + " does not match video size";
+			return false;
+		}
+		if (o + frame.size() > v.data.size()) v.data.resize(o + frame.size());
+		std::copy(frame.begin(), frame.end(), v.data.begin() + o);
+		o += frame.size();
+	}
+	return true;
+}
+
+bool save_video(const std::string &pattern, unsigned first, unsigned step, const Video &v, std::string &err)
+{
+	const size_t whc = (size_t)v.w * v.h * v.c;
+	for (unsigned k = 0; k < v.f; k++) {
+		char name[1024];
+		std::snprintf(name, sizeof name, pattern.c_str(), first + k * step);
+		if (!write_frame(name, v.data.data() + k * whc, v.w, v.h, v.c)) {
+			err = "Video<T>::saveVideo: writing of " + std::string(name) + " failed";
+			return false;
+		}
+	}
+	return true;
+}
+
 bool read_grey(const char *path, std::vector<float> &out, int &w, int &h, std::string &why)
 {
 	const std::string p(path);

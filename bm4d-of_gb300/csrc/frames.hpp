@@ -25,6 +25,23 @@
 namespace bm4dof_frames {
 
 bool read_frame(const char *path, std::vector<float> &out, int &w, int &h, int &c);
+
+// A video as the command lines hold it: planar frames (c, y, x), frame after
+// frame, like the reference's Video<float> (src/utils/lib_videot.hpp:134-181).
+struct Video {
+	std::vector<float> data;
+	unsigned w = 0, h = 0, c = 0, f = 0;
+};
+
+// Video<float>::loadVideo (src/utils/lib_videot.cpp:30-89): frames first,
+// first+step, ... up to last, named by the printf pattern; (last-first+1)/step
+// frames; err receives the reference's message on failure.
+bool load_video(const std::string &pattern, unsigned first, unsigned last, unsigned step, Video &v,
+                std::string &err);
+
+// Video<float>::saveVideo (src/utils/lib_videot.cpp:91-126): v.f frames named
+// first, first+step, ..., written by write_frame (no clipping).
+bool save_video(const std::string &pattern, unsigned first, unsigned step, const Video &v, std::string &err);
 bool write_frame(const char *path, const float *planar, int w, int h, int c);
 
 // One grey frame as the reference's optical-flow tool reads it
