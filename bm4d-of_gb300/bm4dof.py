@@ -43,7 +43,8 @@ EXPORTS = [
     "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run", "bm4dof_process",
     "bm4dof_get_groups", "bm4dof_last_timings", "bm4dof_search_groups_noalloc",
     "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_gain_samples",
-    "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_params", "bm4dof_trainer_grad",
+    "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_params", "bm4dof_trainer_state",
+    "bm4dof_trainer_grad",
     "bm4dof_trainer_step", "bm4dof_trainer_predict", "bm4dof_run_batched", "bm4dof_autotune",
     "bm4dof_tvl1_default_params", "bm4dof_tvl1_pairs", "bm4dof_tvl1_video",
 ]
@@ -190,6 +191,9 @@ def load(path: str = LIB_PATH):
     L.bm4dof_trainer_destroy.restype = None
     L.bm4dof_trainer_params.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
     L.bm4dof_trainer_params.restype = C.c_int
+    L.bm4dof_trainer_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                       C.POINTER(C.c_ulonglong), C.c_int]
+    L.bm4dof_trainer_state.restype = C.c_int
     L.bm4dof_trainer_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint, C.c_void_p,
                                       C.POINTER(C.c_float)]
     L.bm4dof_trainer_grad.restype = C.c_int
@@ -544,6 +548,32 @@ class Trainer:
         a = np.ascontiguousarray(a, np.float32).ravel()
         _check(load().bm4dof_trainer_params(self._h, C.c_void_p(a.ctypes.data), a.size, 1))
 
+    def state(self):
+        """AdamW state: (first moment, second moment, steps taken)."""
+        m1, m2 = np.zeros(GAIN_PARAMS, np.float32), np.zeros(GAIN_PARAMS, np.float32)
+        steps = C.c_ulonglong()
+        _check(load().bm4dof_trainer_state(self._h, C.c_void_p(m1.ctypes.data), C.c_void_p(m2.ctypes.data),
+                                           GAIN_PARAMS, C.byref(steps), 0))
+        return m1, m2, steps.value
+
+    def set_state(self, m1, m2, steps):
+        m1 = np.ascontiguousarray(m1, np.float32).ravel()
+        m2 = np.ascontiguousarray(m2, np.float32).ravel()
+        n = C.c_ulonglong(int(steps))
+        _check(load().bm4dof_trainer_state(self._h, C.c_void_p(m1.ctypes.data), C.c_void_p(m2.ctypes.data),
+                                           m1.size, C.byref(n), 1))
+
+    def checkpoint(self, path):
+        """Parameters and AdamW state to a host file (save_checkpoint)."""
+        save_checkpoint(path, self.params(), *self.state(), batch=self.batch)
+
+    def restore(self, path):
+        """Parameters and AdamW state from a file written by checkpoint: the
+        next step is the one an uninterrupted run would have taken."""
+        ck = load_checkpoint(path)
+        self.set_params(ck["params"])
+        self.set_state(ck["moment1"], ck["moment2"], ck["steps"])
+
     def grad(self, feat, target):
         g = np.zeros(GAIN_PARAMS, np.float32)
         loss = C.c_float()
@@ -565,6 +595,31 @@ class Trainer:
         _check(load().bm4dof_trainer_predict(self._h, C.c_void_p(feat.data_ptr()), feat.shape[0],
                                              C.c_void_p(out.data_ptr())))
         return out
+
+
+CHECKPOINT_VERSION = 1
+
+
+def save_checkpoint(path, params, moment1, moment2, steps, batch=0):
+    """Gain-network training checkpoint: FP32 parameters, AdamW moments (laid
+    out like the parameters) and step count in one .npz file."""
+    arrs = [np.ascontiguousarray(a, np.float32).ravel() for a in (params, moment1, moment2)]
+    if any(a.size != GAIN_PARAMS for a in arrs):
+        raise ValueError(f"checkpoint blobs hold {GAIN_PARAMS} floats each")
+    with open(path, "wb") as f:
+        np.savez(f, version=np.array(CHECKPOINT_VERSION), params=arrs[0], moment1=arrs[1], moment2=arrs[2],
+                 steps=np.array(int(steps), np.uint64), batch=np.array(int(batch), np.uint64))
+
+
+def load_checkpoint(path):
+    with np.load(path) as z:
+        if int(z["version"]) != CHECKPOINT_VERSION:
+            raise ValueError(f"{path}: checkpoint version {int(z['version'])}, expected {CHECKPOINT_VERSION}")
+        ck = {k: z[k].copy() for k in ("params", "moment1", "moment2")}
+        ck["steps"], ck["batch"] = int(z["steps"]), int(z["batch"])
+    if any(ck[k].size != GAIN_PARAMS for k in ("params", "moment1", "moment2")):
+        raise ValueError(f"{path}: checkpoint blobs hold {GAIN_PARAMS} floats each")
+    return ck
 
 
 def split_params(a):

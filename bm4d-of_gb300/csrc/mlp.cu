@@ -555,6 +555,36 @@ bm4dof_status bm4dof_trainer_params(bm4dof_trainer *t, float *params, size_t n, 
 	return BM4DOF_OK;
 }
 
+bm4dof_status bm4dof_trainer_state(bm4dof_trainer *t, float *moment1, float *moment2, size_t n,
+                                   unsigned long long *steps, int set)
+{
+	clear_error();
+	if (!t || !moment1 || !moment2 || !steps || n != (size_t)kMlpPublicSize) {
+		set_error("bm4dof_trainer_state: bad argument (each moment holds " + std::to_string(kMlpPublicSize) +
+		          " floats)");
+		return BM4DOF_ERR_ARGUMENT;
+	}
+	TCK(cudaSetDevice(t->device));
+	std::vector<float> m1(kMlpMasterSize), m2(kMlpMasterSize);
+	if (set) {
+		// the padded inputs of W1 never receive a gradient: their moments stay 0
+		mlp_public_to_master(moment1, m1.data());
+		mlp_public_to_master(moment2, m2.data());
+		TCK(cudaMemcpyAsync(t->m1, m1.data(), sizeof(float) * kMlpMasterSize, cudaMemcpyHostToDevice, t->st));
+		TCK(cudaMemcpyAsync(t->m2, m2.data(), sizeof(float) * kMlpMasterSize, cudaMemcpyHostToDevice, t->st));
+		TCK(cudaStreamSynchronize(t->st));
+		t->step = (long long)*steps;
+	} else {
+		TCK(cudaMemcpyAsync(m1.data(), t->m1, sizeof(float) * kMlpMasterSize, cudaMemcpyDeviceToHost, t->st));
+		TCK(cudaMemcpyAsync(m2.data(), t->m2, sizeof(float) * kMlpMasterSize, cudaMemcpyDeviceToHost, t->st));
+		TCK(cudaStreamSynchronize(t->st));
+		mlp_master_to_public(m1.data(), moment1);
+		mlp_master_to_public(m2.data(), moment2);
+		*steps = (unsigned long long)t->step;
+	}
+	return BM4DOF_OK;
+}
+
 bm4dof_status bm4dof_trainer_grad(bm4dof_trainer *t, const float *feat, const float *target, unsigned n,
                                   float *grads, float *loss)
 {

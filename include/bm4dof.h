@@ -353,6 +353,12 @@ bm4dof_status bm4dof_trainer_create(bm4dof_trainer **t, int device, unsigned bat
 void          bm4dof_trainer_destroy(bm4dof_trainer *t);
 /* Reads (set = 0) or writes (set = 1) the FP32 master parameters as a host blob. */
 bm4dof_status bm4dof_trainer_params(bm4dof_trainer *t, float *params, size_t n, int set);
+/* Reads (set = 0) or writes (set = 1) the AdamW state for a checkpoint: the
+ * first and second moments (host blobs laid out like the parameters) and the
+ * number of steps taken.  Restored with the parameters, training continues
+ * exactly as if it had not stopped. */
+bm4dof_status bm4dof_trainer_state(bm4dof_trainer *t, float *moment1, float *moment2, size_t n,
+                                   unsigned long long *steps, int set);
 /* Loss and gradient (host blob, may be NULL) of one batch, no update. */
 bm4dof_status bm4dof_trainer_grad(bm4dof_trainer *t, const float *feat, const float *target, unsigned n,
                                   float *grads, float *loss);
