@@ -34,6 +34,17 @@ void swap4(unsigned char *p)
 	std::swap(p[1], p[2]);
 }
 
+// bytes from the current position to the end of the file: a corrupt header
+// cannot ask for more memory than the file holds
+size_t remaining(FILE *f)
+{
+	const long here = std::ftell(f);
+	if (here < 0 || std::fseek(f, 0, SEEK_END) != 0) return 0;
+	const long end = std::ftell(f);
+	std::fseek(f, here, SEEK_SET);
+	return end > here ? (size_t)(end - here) : 0;
+}
+
 // planar (c, y, x) floats
 bool read_pfm(const char *path, std::vector<float> &out, int &w, int &h, int &c)
 {
@@ -46,6 +57,7 @@ bool read_pfm(const char *path, std::vector<float> &out, int &w, int &h, int &c)
 	c = tag[1] == 'F' ? 3 : 1;
 	ok = ok && tag[0] == 'P' && (tag[1] == 'F' || tag[1] == 'f');
 	std::vector<unsigned char> raw;
+	if (ok) ok = (size_t)w * h * c * 4 <= remaining(f);
 	if (ok) {
 		raw.resize((size_t)w * h * c * 4);
 		ok = std::fread(raw.data(), 1, raw.size(), f) == raw.size();
@@ -91,6 +103,7 @@ bool read_flo(const char *path, std::vector<float> &out, int &w, int &h, int &c)
 	h = wh[1];
 	c = 2;
 	std::vector<float> raw;
+	if (ok) ok = (size_t)w * h * 2 * sizeof(float) <= remaining(f);
 	if (ok) {
 		raw.resize((size_t)w * h * 2);
 		ok = std::fread(raw.data(), sizeof(float), raw.size(), f) == raw.size();
@@ -274,6 +287,7 @@ bool read_tiff(const char *path, std::vector<float> &out, int &w, int &h, int &c
 	c = (int)spp;
 	if (sample) *sample = fmt == 3 ? 0 : (int)bits;
 	const size_t bytes = bits / 8, wh = (size_t)w * h;
+	if (wh * c * bytes > b.size()) return false;   // more samples than the file holds
 	// the strips, in order, hold the samples in file order
 	std::vector<unsigned char> data;
 	data.reserve(wh * c * bytes);

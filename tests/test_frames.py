@@ -214,3 +214,34 @@ def test_flow_written_as_flo_or_tiff(convert, tmp_path):
     dst = tmp_path / "out.tif"
     assert subprocess.run([convert, "-flow", str(src), str(dst)], capture_output=True).returncode == 0
     assert np.array_equal(read_float_tiff(dst), uv)
+
+
+def test_corrupt_files_are_refused(convert, tmp_path):
+    # host-side fault injection: truncated data, a wrong magic number and
+    # headers that promise more samples than the file holds are read errors,
+    # never an allocation of the promised size or a crash
+    dst = str(tmp_path / "o.pfm")
+    cases = {
+        "short.flo": struct.pack("<fii", 202021.25, 4, 3) + bytes(4 * 2 * 11),
+        "magic.flo": struct.pack("<fii", 1.0, 4, 3) + bytes(4 * 2 * 12),
+        "huge.flo": struct.pack("<fii", 202021.25, 1 << 30, 1 << 30) + bytes(64),
+        "short.pfm": b"Pf\n4 3\n-1.0\n" + bytes(4 * 11),
+        "huge.pfm": b"PF\n1073741824 1073741824\n-1.0\n" + bytes(64),
+        "empty.pfm": b"",
+    }
+    for name, data in cases.items():
+        (tmp_path / name).write_bytes(data)
+        r = subprocess.run([convert, str(tmp_path / name), dst], capture_output=True, text=True)
+        assert r.returncode == 3, (name, r.returncode, r.stderr)
+    # a TIFF whose width and height promise far more samples than its strip
+    src = tmp_path / "huge.tif"
+    write_tiff(src, np.zeros((1, 4, 4), np.float32), np.float32)
+    b = bytearray(open(src, "rb").read())
+    n = struct.unpack_from("<H", b, 8)[0]
+    for i in range(n):
+        tag = struct.unpack_from("<H", b, 10 + 12 * i)[0]
+        if tag in (256, 257):
+            struct.pack_into("<I", b, 10 + 12 * i + 8, 1 << 30)
+    open(src, "wb").write(bytes(b))
+    r = subprocess.run([convert, str(src), dst], capture_output=True, text=True)
+    assert r.returncode == 3, r.stderr
