@@ -41,6 +41,7 @@ EXPORTS = [
     "bm4dof_initialize_params", "bm4dof_set_size_search_window", "bm4dof_set_size_patch",
     "bm4dof_set_n_similar_patches", "bm4dof_format_params", "bm4dof_print_params",
     "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run", "bm4dof_process",
+    "bm4dof_set_memory_limit",
     "bm4dof_get_groups", "bm4dof_last_timings", "bm4dof_search_groups_noalloc",
     "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_gain_samples",
     "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_params", "bm4dof_trainer_state",
@@ -155,6 +156,8 @@ def load(path: str = LIB_PATH):
                                  C.c_uint, C.c_void_p, C.c_void_p, C.POINTER(Params), C.POINTER(Crop), C.c_uint,
                                  C.POINTER(C.c_uint)]
     L.bm4dof_process.restype = C.c_int
+    L.bm4dof_set_memory_limit.argtypes = [C.c_void_p, C.c_size_t]
+    L.bm4dof_set_memory_limit.restype = C.c_int
     L.bm4dof_get_groups.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.POINTER(C.c_uint), C.POINTER(C.c_uint),
                                     C.POINTER(C.c_uint), C.c_uint, C.c_size_t, C.POINTER(C.c_size_t)]
     L.bm4dof_get_groups.restype = C.c_int
@@ -440,6 +443,10 @@ class Context:
             break
         keep = valid[: n.value].bool()
         return feat[: n.value][keep], tgt[: n.value][keep]
+
+    def set_memory_limit(self, nbytes):
+        """Cap on the device memory this context holds (0: none)."""
+        _check(load().bm4dof_set_memory_limit(self._h, int(nbytes)))
 
     def processNlBayes(self, noisy, fflow, bflow, params, crop=None, basic=None, mixed=False, vbm3d=False,
                        keep_groups=False):

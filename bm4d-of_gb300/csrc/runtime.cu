@@ -62,6 +62,7 @@ struct bm4dof_ctx {
 	bool no_marks = false;       // inside a graph capture: no timing events
 	int search_ctas = 0;         // exact search CTAs per SM (0: default)
 	size_t held = 0;          // device bytes held in bufs
+	size_t mem_limit = 0;     // cap on held (0: none), bm4dof_set_memory_limit
 	float whf = 1.f;          // W*H*F of the current run
 	bm4dof_ctx_ext *x = nullptr;
 };
@@ -85,6 +86,12 @@ bm4dof_status dbuf(bm4dof_ctx *ctx, const char *name, size_t count, T **out)
 	DevBuf &b = ctx->bufs[name];
 	const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
 	if (b.cap < bytes) {
+		if (ctx->mem_limit && ctx->held - b.cap + bytes > ctx->mem_limit) {
+			set_error(std::string("device memory limit of ") + std::to_string(ctx->mem_limit) + " bytes reached: " +
+			          name + " needs " + std::to_string(bytes) + " bytes beside " +
+			          std::to_string(ctx->held - b.cap) + " held");
+			return BM4DOF_ERR_NO_MEMORY;
+		}
 		if (b.p) cudaFree(b.p);
 		ctx->held -= b.cap;
 		b.p = nullptr;
@@ -381,6 +388,7 @@ void set_budget(bm4dof_ctx *ctx)
 	size_t freeb = 0, totalb = 0;
 	if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess && budget > (freeb + ctx->held) / 2)
 		budget = (freeb + ctx->held) / 2;
+	if (ctx->mem_limit && budget > ctx->mem_limit / 4) budget = ctx->mem_limit / 4;
 	ctx->slot_budget = budget;
 }
 
@@ -1103,6 +1111,17 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
 	CK(cudaStreamSynchronize(ctx->st));
 	collect_times(ctx);
 	return finish_run(ctx, r, ratios);
+}
+
+bm4dof_status bm4dof_set_memory_limit(bm4dof_ctx *ctx, size_t bytes)
+{
+	clear_error();
+	if (!ctx) {
+		set_error("bm4dof_set_memory_limit: null context");
+		return BM4DOF_ERR_ARGUMENT;
+	}
+	ctx->mem_limit = bytes;
+	return BM4DOF_OK;
 }
 
 bm4dof_status bm4dof_process(bm4dof_ctx *ctx, const float *noisy, const float *fflow, const float *bflow,

@@ -119,6 +119,13 @@ typedef struct bm4dof_ctx bm4dof_ctx;
 bm4dof_status bm4dof_create(bm4dof_ctx **ctx, int device);
 void          bm4dof_destroy(bm4dof_ctx *ctx);
 
+/* Caps the device memory the context's buffers may hold (0: no cap, the
+ * default).  A call that would need more fails with BM4DOF_ERR_NO_MEMORY and
+ * a message naming the buffer; the context stays usable.  The chunk budget of
+ * the aggregation terms shrinks with the cap.  Applies to the calls made on
+ * this context (not to the private contexts of bm4dof_run_batched). */
+bm4dof_status bm4dof_set_memory_limit(bm4dof_ctx *ctx, size_t bytes);
+
 /* Flags for bm4dof_run. */
 #define BM4DOF_DEVICE_POINTERS  0x1u  /* all video pointers are device pointers  */
 #define BM4DOF_KEEP_GROUPS      0x2u  /* record neighbour lists for inspection   */
