@@ -525,6 +525,14 @@ def runNlBayes(noisy, fflow, bflow, p1, p2, basic=None, nparts=2, **kw):
     return _default.runNlBayes(noisy, fflow, bflow, p1, p2, basic=basic, nparts=nparts, **kw)
 
 
+def processNlBayes(noisy, fflow, bflow, params, crop=None, basic=None, **kw):
+    """Module-level VideoNLB::processNlBayes on device 0."""
+    global _default
+    if _default is None:
+        _default = Context(0)
+    return _default.processNlBayes(noisy, fflow, bflow, params, crop=crop, basic=basic, **kw)
+
+
 class Trainer:
     """GPU training of the gain network (bm4dof_trainer_*): BF16 forward and
     backward with FP32 accumulation, AdamW on FP32 master weights.  Features
