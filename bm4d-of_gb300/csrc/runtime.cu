@@ -16,6 +16,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -63,11 +64,22 @@ struct bm4dof_ctx {
 	int search_ctas = 0;         // exact search CTAs per SM (0: default)
 	size_t held = 0;          // device bytes held in bufs
 	size_t mem_limit = 0;     // cap on held (0: none), bm4dof_set_memory_limit
+	std::recursive_mutex mu;  // calls on one context are serialised (CtxLock)
 	float whf = 1.f;          // W*H*F of the current run
 	bm4dof_ctx_ext *x = nullptr;
 };
 
 namespace {
+
+// Held by every entry point that takes a context, so that calls made on one
+// context from several host threads run one after the other.
+struct CtxLock {
+	std::unique_lock<std::recursive_mutex> l;
+	explicit CtxLock(bm4dof_ctx *c)
+	{
+		if (c) l = std::unique_lock<std::recursive_mutex>(c->mu);
+	}
+};
 
 enum { T_SEARCH = 0, T_FILTER = 1, T_AGG = 2, T_OTHER = 3 };
 
@@ -1075,6 +1087,7 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
                          const bm4dof_params *p1, const bm4dof_params *p2, unsigned nparts,
                          unsigned flags, float ratios[2])
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx || !p1 || !p2) {
 		set_error("bm4dof_run: null pointer or empty video");
@@ -1115,6 +1128,7 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
 
 bm4dof_status bm4dof_set_memory_limit(bm4dof_ctx *ctx, size_t bytes)
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx) {
 		set_error("bm4dof_set_memory_limit: null context");
@@ -1129,6 +1143,7 @@ bm4dof_status bm4dof_process(bm4dof_ctx *ctx, const float *noisy, const float *f
                              const bm4dof_params *params, const bm4dof_crop *crop, unsigned flags,
                              unsigned *groups)
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx || !params) {
 		set_error("bm4dof_process: null pointer or empty video");
@@ -1365,6 +1380,7 @@ extern "C" {
 bm4dof_status bm4dof_run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n, unsigned flags,
                                  const bm4dof_tuning *tuning)
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx || !seqs || n == 0) {
 		set_error("bm4dof_run_batched: null context or no sequences");
@@ -1385,6 +1401,7 @@ bm4dof_status bm4dof_run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigne
 bm4dof_status bm4dof_autotune(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n, unsigned sample,
                               unsigned flags, bm4dof_tuning *best, float *table, unsigned cap, unsigned *rows)
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx || !seqs || n == 0 || !best) {
 		set_error("bm4dof_autotune: bad argument");
@@ -1451,6 +1468,7 @@ bm4dof_status bm4dof_get_groups(bm4dof_ctx *ctx, unsigned step, unsigned tile, u
                                 unsigned *nsimp, unsigned *index, unsigned stride, size_t cap,
                                 size_t *count)
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx || step < 1 || step > 2 || !count) { set_error("bm4dof_get_groups: bad argument"); return BM4DOF_ERR_ARGUMENT; }
 	const std::vector<KeptGroups> &kg = ctx->kept[step - 1];
@@ -1470,6 +1488,7 @@ bm4dof_status bm4dof_get_groups(bm4dof_ctx *ctx, unsigned step, unsigned tile, u
 
 bm4dof_status bm4dof_set_gain_network(bm4dof_ctx *ctx, const float *params, size_t n, float kappa)
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx || (params && n != (size_t)kMlpPublicSize) || kappa < 0.f) {
 		set_error("bm4dof_set_gain_network: bad argument (the blob holds " + std::to_string(kMlpPublicSize) +
@@ -1497,6 +1516,7 @@ bm4dof_status bm4dof_set_gain_network(bm4dof_ctx *ctx, const float *params, size
 
 bm4dof_status bm4dof_learned_stats(bm4dof_ctx *ctx, unsigned long long *groups, unsigned long long *fallbacks)
 {
+	CtxLock lock_(ctx);
 	if (!ctx) return BM4DOF_ERR_ARGUMENT;
 	if (groups) *groups = ctx->l_groups;
 	if (fallbacks) *fallbacks = ctx->l_fallbacks;
@@ -1508,6 +1528,7 @@ bm4dof_status bm4dof_gain_samples(bm4dof_ctx *ctx, const float *noisy, const flo
                                   const bm4dof_params *p2, unsigned nparts, unsigned flags, float *feat,
                                   float *target, unsigned char *valid, size_t cap, size_t *count)
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx || !noisy || !basic || !p2 || !feat || !target || !valid || !count || W == 0 || H == 0 || F == 0 ||
 	    (fflow == nullptr) != (bflow == nullptr) || (flags & ~BM4DOF_DEVICE_POINTERS)) {
@@ -1620,6 +1641,7 @@ extern "C" {
 bm4dof_status bm4dof_tvl1_pairs(bm4dof_ctx *ctx, const float *I0, const float *I1, unsigned W, unsigned H,
                                 unsigned n, const bm4dof_tvl1_params *params, float *uv, unsigned flags)
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx || !I0 || !I1 || !uv || W < 2 || H < 2 || n == 0 || (flags & ~BM4DOF_DEVICE_POINTERS)) {
 		set_error("bm4dof_tvl1_pairs: bad argument");
@@ -1661,6 +1683,7 @@ bm4dof_status bm4dof_tvl1_pairs(bm4dof_ctx *ctx, const float *I0, const float *I
 bm4dof_status bm4dof_tvl1_video(bm4dof_ctx *ctx, const float *video, unsigned W, unsigned H, unsigned F,
                                 const bm4dof_tvl1_params *params, float *fflow, float *bflow, unsigned flags)
 {
+	CtxLock lock_(ctx);
 	clear_error();
 	if (!ctx || !video || !fflow || !bflow || W < 2 || H < 2 || F < 2 || (flags & ~BM4DOF_DEVICE_POINTERS)) {
 		set_error("bm4dof_tvl1_video: bad argument (grey video of at least 2 frames)");
@@ -1715,6 +1738,7 @@ bm4dof_status bm4dof_tvl1_video(bm4dof_ctx *ctx, const float *video, unsigned W,
 
 bm4dof_status bm4dof_last_timings(bm4dof_ctx *ctx, float ms[5], unsigned *launches)
 {
+	CtxLock lock_(ctx);
 	if (!ctx) return BM4DOF_ERR_ARGUMENT;
 	if (ms) for (int k = 0; k < 5; k++) ms[k] = ctx->ms[k];
 	if (launches) *launches = ctx->launches;
