@@ -59,6 +59,17 @@ def run(exe, *args):
     return subprocess.run([exe, *map(str, args)], capture_output=True, text=True, timeout=120)
 
 
+def test_layer_header_compiles_without_warnings(gpulib, tmp_path):
+    # the header is included into callers' builds: C++11 and warning-free
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    for std in ("-std=c++11", "-std=c++17"):
+        r = subprocess.run([cxx, std, "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", DRIVER],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, (std, r.stderr)
+
+
 def test_layer_conversion_round_trip(layer):
     r = run(layer, "roundtrip")
     assert r.returncode == 0 and r.stdout.strip() == "roundtrip ok"
