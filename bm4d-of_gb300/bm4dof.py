@@ -41,7 +41,7 @@ EXPORTS = [
     "bm4dof_initialize_params", "bm4dof_set_size_search_window", "bm4dof_set_size_patch",
     "bm4dof_set_n_similar_patches", "bm4dof_format_params", "bm4dof_print_params",
     "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run", "bm4dof_process",
-    "bm4dof_set_memory_limit",
+    "bm4dof_set_memory_limit", "bm4dof_plan",
     "bm4dof_get_groups", "bm4dof_last_timings", "bm4dof_search_groups_noalloc",
     "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_gain_samples",
     "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_params", "bm4dof_trainer_state",
@@ -158,6 +158,10 @@ def load(path: str = LIB_PATH):
     L.bm4dof_process.restype = C.c_int
     L.bm4dof_set_memory_limit.argtypes = [C.c_void_p, C.c_size_t]
     L.bm4dof_set_memory_limit.restype = C.c_int
+    L.bm4dof_plan.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.POINTER(Params), C.POINTER(Crop), C.c_int,
+                              C.c_void_p, C.c_uint, C.c_void_p, C.c_size_t, C.POINTER(C.c_uint),
+                              C.POINTER(C.c_size_t)]
+    L.bm4dof_plan.restype = C.c_int
     L.bm4dof_get_groups.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.POINTER(C.c_uint), C.POINTER(C.c_uint),
                                     C.POINTER(C.c_uint), C.c_uint, C.c_size_t, C.POINTER(C.c_size_t)]
     L.bm4dof_get_groups.restype = C.c_int
@@ -523,6 +527,29 @@ def runNlBayes(noisy, fflow, bflow, p1, p2, basic=None, nparts=2, **kw):
     if _default is None:
         _default = Context(0)
     return _default.runNlBayes(noisy, fflow, bflow, p1, p2, basic=basic, nparts=nparts, **kw)
+
+
+def plan(W, H, F, params, nparts=2, crop=None, process=False):
+    """The reference-patch grid (bm4dof_plan, host only): a list of tiles, each
+    {"box": (ox, oy, w, h), "xs": [...], "ys": [...], "fs": [...]} with
+    tile-local positions."""
+    nt, nc = C.c_uint(), C.c_size_t()
+    cr = None if crop is None else C.byref(crop)
+    _check(load().bm4dof_plan(W, H, F, nparts, C.byref(params), cr, int(process), None, 0, None, 0,
+                              C.byref(nt), C.byref(nc)))
+    tiles = np.zeros(7 * nt.value, np.int32)
+    coords = np.zeros(max(nc.value, 1), np.int32)
+    _check(load().bm4dof_plan(W, H, F, nparts, C.byref(params), cr, int(process),
+                              C.c_void_p(tiles.ctypes.data), nt.value, C.c_void_p(coords.ctypes.data), nc.value,
+                              C.byref(nt), C.byref(nc)))
+    out, o = [], 0
+    for i in range(nt.value):
+        ox, oy, w, h, nx, ny, nf = (int(v) for v in tiles[7 * i:7 * i + 7])
+        xs = coords[o:o + nx].tolist(); o += nx
+        ys = coords[o:o + ny].tolist(); o += ny
+        fs = coords[o:o + nf].tolist(); o += nf
+        out.append({"box": (ox, oy, w, h), "xs": xs, "ys": ys, "fs": fs})
+    return out
 
 
 def processNlBayes(noisy, fflow, bflow, params, crop=None, basic=None, **kw):

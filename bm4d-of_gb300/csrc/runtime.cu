@@ -264,6 +264,20 @@ void make_plan(Plan &pl, unsigned W, unsigned H, unsigned F, unsigned nparts, co
 		}
 }
 
+// The crop's sides that stop short of its source (nldct.cpp:520-525), in
+// make_plan's order {x0, y0, t0, x1, y1, t1}; no crop: no border.
+void crop_borders(const bm4dof_crop *crop, int b[6])
+{
+	for (int k = 0; k < 6; k++) b[k] = 0;
+	if (!crop) return;
+	b[0] = crop->origin_x > 0;
+	b[1] = crop->origin_y > 0;
+	b[2] = crop->origin_t > 0;
+	b[3] = crop->ending_x < (int)crop->source_sz.width;
+	b[4] = crop->ending_y < (int)crop->source_sz.height;
+	b[5] = crop->ending_t < (int)crop->source_sz.frames;
+}
+
 Image image(float *p, unsigned W, unsigned H, unsigned C, unsigned F)
 {
 	Image im;
@@ -1126,6 +1140,37 @@ bm4dof_status bm4dof_run(bm4dof_ctx *ctx, const float *noisy, const float *fflow
 	return finish_run(ctx, r, ratios);
 }
 
+bm4dof_status bm4dof_plan(unsigned W, unsigned H, unsigned F, unsigned nparts, const bm4dof_params *params,
+                          const bm4dof_crop *crop, int process, int *tiles, unsigned tiles_cap, int *coords,
+                          size_t coords_cap, unsigned *ntiles, size_t *ncoords)
+{
+	clear_error();
+	if (!params || !ntiles || !ncoords || W == 0 || H == 0 || F == 0 || params->offSet == 0 ||
+	    params->offSetTime == 0 || params->sizePatch == 0 || params->sizePatchTime == 0) {
+		set_error("bm4dof_plan: bad argument");
+		return BM4DOF_ERR_ARGUMENT;
+	}
+	int borders[6];
+	crop_borders(crop, borders);
+	Plan pl;
+	make_plan(pl, W, H, F, nparts ? nparts : 2, *params, process ? borders : nullptr);
+	*ntiles = (unsigned)pl.tiles.size();
+	size_t n = 0;
+	for (size_t i = 0; i < pl.tiles.size(); i++) {
+		const Tile &T = pl.tiles[i];
+		if (tiles && i < tiles_cap) {
+			const int v[7] = {T.ox, T.oy, T.w, T.h, T.nx, T.ny, T.nf};
+			for (int k = 0; k < 7; k++) tiles[7 * i + k] = v[k];
+		}
+		const int offs[3] = {T.gx, T.gy, T.gf}, cnt[3] = {T.nx, T.ny, T.nf};
+		for (int a = 0; a < 3; a++)
+			for (int j = 0; j < cnt[a]; j++, n++)
+				if (coords && n < coords_cap) coords[n] = pl.grid[offs[a] + j];
+	}
+	*ncoords = n;
+	return BM4DOF_OK;
+}
+
 bm4dof_status bm4dof_set_memory_limit(bm4dof_ctx *ctx, size_t bytes)
 {
 	CtxLock lock_(ctx);
@@ -1172,16 +1217,8 @@ bm4dof_status bm4dof_process(bm4dof_ctx *ctx, const float *noisy, const float *f
 	r.flags = flags;
 	bm4dof_status e = validate_run(r, "bm4dof_process");
 	if (e != BM4DOF_OK) return e;
-	// the crop's sides that stop short of its source (nldct.cpp:520-525)
-	int borders[6] = {0, 0, 0, 0, 0, 0};
-	if (crop) {
-		borders[0] = crop->origin_x > 0;
-		borders[1] = crop->origin_y > 0;
-		borders[2] = crop->origin_t > 0;
-		borders[3] = crop->ending_x < (int)crop->source_sz.width;
-		borders[4] = crop->ending_y < (int)crop->source_sz.height;
-		borders[5] = crop->ending_t < (int)crop->source_sz.frames;
-	}
+	int borders[6];
+	crop_borders(crop, borders);
 	r.mode.borders = borders;
 	r.yuv1 = r.yuv2 = false;   // no colour transform of its own
 	CK(cudaSetDevice(ctx->device));

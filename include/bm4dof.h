@@ -191,6 +191,18 @@ bm4dof_status bm4dof_process(bm4dof_ctx *ctx,
                              float *basic, float *final_, const bm4dof_params *params,
                              const bm4dof_crop *crop, unsigned flags, unsigned *groups);
 
+/* The reference-patch grid (host only, no device): the tiles bm4dof_run makes
+ * for nparts (process = 0; subDivideTight, lib_videot.hpp:853-916), or the one
+ * tile of bm4dof_process with crop (process = 1), and in each the reference
+ * patches' positions of nldct.cpp:520-553.  tiles receives 7 ints per tile
+ * {ox, oy, w, h, nx, ny, nf} (at most tiles_cap tiles), coords each tile's nx
+ * x positions, ny y positions and nf frames in turn (at most coords_cap ints,
+ * tile-local); *ntiles and *ncoords receive the full counts.  A tile's groups
+ * are all (x, y, t) of its lists. */
+bm4dof_status bm4dof_plan(unsigned width, unsigned height, unsigned frames, unsigned nparts,
+                          const bm4dof_params *params, const bm4dof_crop *crop, int process, int *tiles,
+                          unsigned tiles_cap, int *coords, size_t coords_cap, unsigned *ntiles, size_t *ncoords);
+
 /* Neighbour lists of the last bm4dof_run made with BM4DOF_KEEP_GROUPS, for one
  * step (1 or 2) and tile.  For each processed group in processing order:
  *   ref[g]          reference patch index (tile video index at channel 0, as

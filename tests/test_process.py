@@ -127,3 +127,60 @@ def test_gpu_process_rejects_the_learned_form(gpulib, gpuctx):
         gpulib._check(gpulib.load().bm4dof_process(gpuctx._h, C.c_void_p(noisy.ctypes.data), None, None, W, H, Cc,
                                                    F, C.c_void_p(out.ctypes.data), C.c_void_p(out.ctypes.data),
                                                    C.byref(p1), None, flags, C.byref(n)))
+
+
+def grid_axis(n, ori, end, step, edge_first, edge_last):
+    """One axis of the reference-patch grid, nldct.cpp:536-547: every step-th
+    position from ori, plus the last one (end - 1) on a side with no border,
+    plus the first one on a side with no border (x and y only)."""
+    return [v for d, v in enumerate(range(ori, end))
+            if d % step == 0 or (edge_last and v == end - 1) or (edge_first and v == ori)]
+
+
+def expected_grid(w, h, F, p, b):
+    """The grid of one tile w x h x F with borders b = (x0, y0, t0, x1, y1, t1)."""
+    sPx, sPt, sWx = p.sizePatch, p.sizePatchTime, p.sizeSearchWindow
+    sWt = p.sizeSearchTimeRangeFwd + p.sizeSearchTimeRangeBwd + 1
+    ox = sPx - 1 + sWx // 2 if b[0] else 0
+    oy = sPx - 1 + sWx // 2 if b[1] else 0
+    of = sPt - 1 + sWt // 2 if b[2] else 0
+    ex = w - (sPx - 1 + sWx // 2 if b[3] else sPx - 1)
+    ey = h - (sPx - 1 + sWx // 2 if b[4] else sPx - 1)
+    ef = F - (sPt - 1 + sWt // 2 if b[5] else sPt - 1)
+    return (grid_axis(w, ox, ex, p.offSet, not b[0], not b[3]), grid_axis(h, oy, ey, p.offSet, not b[1], not b[4]),
+            grid_axis(F, of, ef, p.offSetTime, False, not b[5]))
+
+
+@pytest.mark.parametrize("case", PROCESS_CASES, ids=IDS)
+def test_plan_of_a_crop_is_the_references_grid(gpulib, case):
+    # the host plan bm4dof_process runs on (bm4dof_plan, no device needed)
+    g = load(case[0])
+    F, _, H, W = g["noisy"].shape
+    crop_arr = [int(v) for v in g["crop"]]
+    crop = crop_of(gpulib, g["crop"])
+    if crop is None:
+        b = (0,) * 6
+    else:
+        o, e, s = crop_arr[0:3], crop_arr[3:6], crop_arr[6:9]
+        b = (o[0] > 0, o[1] > 0, o[2] > 0, e[0] < s[0], e[1] < s[1], e[2] < s[2])
+    for tag in ("p1", "p2"):
+        p = params(gpulib, g[tag])
+        (t,) = gpulib.plan(W, H, F, p, crop=crop, process=True)
+        assert t["box"] == (0, 0, W, H)
+        assert (t["xs"], t["ys"], t["fs"]) == expected_grid(W, H, F, p, b), (case[0], tag)
+
+
+@pytest.mark.parametrize("nparts", [1, 2, 4, 6, 8])
+def test_plan_of_a_run_is_the_references_tiling_and_grid(gpulib, oracle, nparts):
+    W, H, F = 70, 52, 7
+    size = (W, H, F, 1)
+    p = gpulib.initializeNlbParameters(2, 20.0, size)
+    gpulib.setSizePatch(p, size, 4)
+    p.sizePatchTime = 2
+    tiles = gpulib.plan(W, H, F, p, nparts=nparts)
+    boxes = oracle.tile_crops(W, H, nparts, int(p.boundary))      # subDivideTight, pinned to the reference
+    assert len(tiles) == len(boxes)
+    for t, (ox, oy, ex, ey) in zip(tiles, boxes.tolist()):
+        assert t["box"] == (ox, oy, ex - ox, ey - oy)
+        b = (ox > 0, oy > 0, False, ex < W, ey < H, False)
+        assert (t["xs"], t["ys"], t["fs"]) == expected_grid(ex - ox, ey - oy, F, p, b)
