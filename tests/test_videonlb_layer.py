@@ -140,6 +140,18 @@ def test_gpu_layer_run_equals_the_library(layer, gpulib, gpuctx, tmp_path):
     assert [float(x) for x in r.stdout.split()] == pytest.approx([float(x) for x in ratios], abs=1e-5)
 
 
+def test_layer_tile_count_follows_openmp(layer):
+    # 2 x omp_get_max_threads() as the reference (nldct.cpp:318-323): from
+    # OMP_NUM_THREADS when set, else the host's hardware threads
+    env = {k: v for k, v in os.environ.items() if k != "OMP_NUM_THREADS"}
+    r = subprocess.run([layer, "tiles"], capture_output=True, text=True, env=dict(env, OMP_NUM_THREADS="3"))
+    assert r.stdout.strip() == "6"
+    r = subprocess.run([layer, "tiles"], capture_output=True, text=True, env=dict(env, OMP_NUM_THREADS="4,2"))
+    assert r.stdout.strip() == "8"
+    r = subprocess.run([layer, "tiles"], capture_output=True, text=True, env=env)
+    assert r.stdout.strip() == str(2 * (os.cpu_count() or 1))
+
+
 def test_layer_process_refuses_sizes_it_cannot_read(layer):
     r = run(layer, "process_errors")
     assert r.returncode == 0, r.stderr

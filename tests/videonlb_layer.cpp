@@ -10,6 +10,7 @@
 //   videonlb_layer roundtrip   field-for-field conversion both ways
 //   videonlb_layer errors      runNlBayes on inputs the reference rejects
 //   videonlb_layer process_errors   processNlBayes on inputs the layer refuses
+//   videonlb_layer tiles       the tile count runNlBayes uses without one
 //   videonlb_layer run W H C F sigma nparts noisy.raw basic.raw final.raw
 //                              one denoising run (needs a GPU), planar floats
 //   videonlb_layer process W H C F sigma noisy.raw basic.raw final.raw
@@ -314,6 +315,7 @@ int main(int argc, char **argv)
 	if (c == "roundtrip") return cmd_roundtrip();
 	if (c == "errors") return cmd_errors();
 	if (c == "process_errors") return cmd_process_errors();
+	if (c == "tiles") return std::printf("%u\n", L::default_tiles()), 0;
 	if (c == "run" && argc == 11) return cmd_run(argv + 2);
 	if (c == "process" && argc == 19) return cmd_process(argv + 2);
 	std::fprintf(stderr, "usage: videonlb_layer params|roundtrip|errors|process_errors|run|process ...\n");
