@@ -2,6 +2,7 @@
 """Training of the learned form's gain network on the GPU.
 
     python bm4d-of_gb300/train_gains.py [--clips 2000] [--epochs 12] [--out FILE]
+                                        [--checkpoint FILE [--resume]]
 
 Training pairs come from the plain two-step method itself: each seeded
 synthetic grey clip (64x64x8, sigma uniform in [5, 50], the cosine+rectangle
@@ -13,6 +14,12 @@ basic estimate.  The network is trained with the library's BF16 forward,
 backward and AdamW kernels (bm4dof_trainer_*), cosine learning-rate decay, and
 saved as a float32 blob (BM4DOF_GAIN_PARAMS values, bm4dof.split_params
 layout) in an .npz together with its training record.
+
+With --checkpoint the trainer's parameters and AdamW state are written to
+FILE after every epoch (Trainer.checkpoint), with the epoch count and the best
+validation epoch beside it in FILE.json; --resume restores them and continues
+with the next epoch (the shuffles of the finished epochs are replayed, so the
+run takes the steps an uninterrupted one would have taken).
 
 The last 5 % of the clips are held out for the validation loss.  The record
 also holds PSNR on a held-out 256x256x12 clip at sigma 20: plain method,
@@ -91,9 +98,10 @@ def evaluate(ctx, params, W=256, H=256, F=12, sigma=20.0, seed=424242, kappa=0.0
     return out
 
 
-def train(feat, tgt, epochs, batch, lr, wd, seed, val=None, log=print):
+def train(feat, tgt, epochs, batch, lr, wd, seed, val=None, log=print, checkpoint=None, resume=False):
     """AdamW with cosine decay; returns the trainer holding the parameters of
-    the epoch with the lowest validation loss (the last epoch without val)."""
+    the epoch with the lowest validation loss (the last epoch without val).
+    checkpoint: file written after every epoch; resume: continue from it."""
     import torch
     tr = bm4dof.Trainer(batch=batch, seed=seed)
     n = feat.shape[0]
@@ -103,7 +111,19 @@ def train(feat, tgt, epochs, batch, lr, wd, seed, val=None, log=print):
     step = 0
     history, vhist = [], []
     best = (float("inf"), None)
-    for e in range(epochs):
+    start = 0
+    if checkpoint and resume and os.path.exists(checkpoint):
+        tr.restore(checkpoint)
+        with open(checkpoint + ".json") as f:
+            meta = json.load(f)
+        start, history, vhist = meta["epochs_done"], meta["train_loss"], meta["val_loss_per_epoch"]
+        if meta.get("best_val") is not None:
+            best = (meta["best_val"], bm4dof.load_checkpoint(checkpoint + ".best.npz")["params"])
+        step = start * per_epoch
+        for _ in range(start):
+            torch.randperm(n, generator=gen)     # the shuffles of the finished epochs
+        log(f"resumed after epoch {start - 1}")
+    for e in range(start, epochs):
         perm = torch.randperm(n, generator=gen).cuda()
         losses = []
         for s in range(per_epoch):
@@ -122,7 +142,14 @@ def train(feat, tgt, epochs, batch, lr, wd, seed, val=None, log=print):
             msg += f"  validation {vl:.5f}"
             if vl < best[0]:
                 best = (vl, tr.params())
+                if checkpoint:
+                    bm4dof.save_checkpoint(checkpoint + ".best.npz", best[1], *tr.state())
         log(msg)
+        if checkpoint:
+            tr.checkpoint(checkpoint)
+            with open(checkpoint + ".json", "w") as f:
+                json.dump({"epochs_done": e + 1, "train_loss": history, "val_loss_per_epoch": vhist,
+                           "best_val": None if best[1] is None else best[0]}, f)
     if best[1] is not None:
         tr.set_params(best[1])
     return tr, history, vhist
@@ -147,6 +174,8 @@ def main():
     ap.add_argument("--wd", type=float, default=1e-4)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--checkpoint", default=None, help="trainer checkpoint written after every epoch")
+    ap.add_argument("--resume", action="store_true", help="continue from --checkpoint")
     args = ap.parse_args()
     import torch
     t0 = time.time()
@@ -157,7 +186,8 @@ def main():
     fva, tva = torch.cat(feats[-nval:]), torch.cat(tgts[-nval:])
     t1 = time.time()
     print(f"dataset: {ftr.shape[0]} train / {fva.shape[0]} validation pairs in {t1 - t0:.1f} s", flush=True)
-    tr, hist, vhist = train(ftr, ttr, args.epochs, args.batch, args.lr, args.wd, args.seed, val=(fva, tva))
+    tr, hist, vhist = train(ftr, ttr, args.epochs, args.batch, args.lr, args.wd, args.seed, val=(fva, tva),
+                            checkpoint=args.checkpoint, resume=args.resume)
     t2 = time.time()
     params = tr.params()
     record = {
