@@ -49,8 +49,10 @@ CLI = dict(px1=4, px2=4, pt1=4, pt2=4, wx1=21, wx2=21, np1=16, np2=16, b1=3.0)
 METRIC = "megapixel-frames/s at 1 GPU, plain vs learned/mixed at ≤0.05 dB PSNR loss"
 UNIT = "MPF/s"
 SEARCH_TRAFFIC_SMALL = 11.24e6 + 0.648e6
-# CPU sample (crop of the same workload) for the host-core baseline
-CPU_SAMPLE = (480, 272, 13)
+# CPU sample (crop of the same workload) for the host-core baseline: 12
+# frames, so that every reference patch has the full 9-frame search range it
+# has in the long video
+CPU_SAMPLE = (480, 272, 12)
 
 
 def resolve(lib, W, H, F, sigma):
@@ -137,9 +139,60 @@ def replica_max_ms(ms, world):
     return float(t.item())
 
 
+def plan_groups(W, H, F, p, nparts):
+    """Reference patches (groups) of one step over all tiles of a run, counted
+    on the host without the GPU library: the tiles of subDivideTight
+    (lib_videot.hpp:853-916, grid from determineFactor, utilities.cpp:137-158)
+    and the reference grid of processNlBayes (nldct.cpp:520-553).
+    tests/test_bench_baseline.py checks it against bm4dof_plan."""
+    if nparts == 1:
+        nw, nh = 1, 1
+    else:
+        nh = 2
+        while nparts % nh:
+            nh += 1
+        nw = nparts // nh
+        if nh > nw:
+            nw, nh = nh, nparts // nh
+    wt = int(np.ceil(np.float32(W) / np.float32(nw)))
+    ht = int(np.ceil(np.float32(H) / np.float32(nh)))
+    N, px, pt, wx = p.boundary, p.sizePatch, p.sizePatchTime, p.sizeSearchWindow
+
+    def count(ori, end, step, b0, b1):
+        return sum(1 for v in range(ori, end)
+                   if (v - ori) % step == 0 or (not b1 and v == end - 1) or (not b0 and v == ori))
+
+    nf = count(0, F - (pt - 1), p.offSetTime, False, False)
+    total = 0
+    for j in range(nh):
+        for i in range(nw):
+            ox, ex = max(0, i * wt - N), min(W, (i + 1) * wt + N)
+            oy, ey = max(0, j * ht - N), min(H, (j + 1) * ht + N)
+            bx0, bx1, by0, by1 = ox > 0, ex < W, oy > 0, ey < H
+            half = px - 1 + wx // 2
+            nx = count(half if bx0 else 0, (ex - ox) - (half if bx1 else px - 1), p.offSet, bx0, bx1)
+            ny = count(half if by0 else 0, (ey - oy) - (half if by1 else px - 1), p.offSet, by0, by1)
+            total += nx * ny * nf
+    return total
+
+
 def cpu_baseline(nz, ff, bf, sigma, threads=None, sample=CPU_SAMPLE):
     """The reference algorithm on the host cores (oracle restatement, OpenMP over
-    the reference's 2*threads tiles) on a crop of the workload."""
+    the reference's 2*threads tiles) on a crop of the workload, scaled to the
+    whole workload by groups.
+
+    The reference's work is proportional to the groups it processes: every
+    group searches the same 21x21x9 candidates (12 sample frames give every
+    group the full temporal range) and filters and aggregates the same patch
+    group, whatever tile it lies in.  The crop's tiles are small, so it
+    processes more groups per pixel (tile halos) than the whole video would,
+    and its few tiles balance unevenly over the threads.  So the CPU time of
+    all threads (user + system) per processed group is measured on the crop
+    (about 2 % apart between a 160x136 and a 480x272 crop, where wall-clock
+    time per group differed by 11 %), and the whole video's time is that
+    per-group cost times the groups the reference processes on it with the
+    same thread count (2*threads tiles of the full frame), divided evenly over
+    the threads: a perfectly balanced run, which no real run beats."""
     import pyoracle
     pyoracle.build()
     O = pyoracle.Oracle()
@@ -147,12 +200,24 @@ def cpu_baseline(nz, ff, bf, sigma, threads=None, sample=CPU_SAMPLE):
     W, H, F = sample
     crop = lambda v: np.ascontiguousarray(v[:F, :, :H, :W])
     p1, p2 = resolve(O, W, H, F, sigma)
+    c0 = os.times()
     t = time.perf_counter()
     O.runNlBayes(crop(nz), crop(ff), crop(bf), p1, p2, nparts=2 * threads, nthreads=threads)
     dt = time.perf_counter() - t
-    return {"value": W * H * F / 1e6 / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{W}x{H}x{F} crop of the same workload, both steps, {dt:.1f} s, "
-                      f"{2 * threads} tiles"}
+    c1 = os.times()
+    cpu_s = (c1.user - c0.user) + (c1.system - c0.system)
+    FW, FH, FF = nz.shape[3], nz.shape[2], nz.shape[0]
+    g_sample = plan_groups(W, H, F, p1, 2 * threads) + plan_groups(W, H, F, p2, 2 * threads)
+    r1, r2 = resolve(O, FW, FH, FF, sigma)
+    g_full = plan_groups(FW, FH, FF, r1, 2 * threads) + plan_groups(FW, FH, FF, r2, 2 * threads)
+    full_s = cpu_s / g_sample * g_full / threads
+    return {"value": FW * FH * FF / 1e6 / full_s, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{W}x{H}x{F} crop of the same workload, both steps, {2 * threads} tiles on {threads} threads: "
+                      f"{dt:.1f} s wall, {cpu_s:.0f} CPU-s for {g_sample} groups ({cpu_s / g_sample * 1e6:.0f} "
+                      f"CPU-us per group); {FW}x{FH}x{FF} at {2 * threads} tiles has {g_full} groups: "
+                      f"{full_s:.0f} s on {threads} threads, perfectly balanced",
+            "sample_value": W * H * F / 1e6 / dt, "cpu_us_per_group": cpu_s / g_sample * 1e6,
+            "groups_sample": g_sample, "groups_full": g_full}
 
 
 def run_reference(args):
@@ -169,10 +234,18 @@ def run_reference(args):
     v = statistics.median(s["value"] for s in samples)
     cb = dict(samples[0])
     cb["value"] = v
+    cfg = config(args)
+    sw, sh, sf = CPU_SAMPLE
+    cfg["workload"] = (f"reference algorithm (oracle restatement) on {cb['cores']} host cores: "
+                       f"{sw}x{sh}x{sf} crop of the grey video {W}x{H}x{F} (sigma {sigma:g}, plain two-step FP32), "
+                       f"{2 * cb['cores']} tiles, timed; its CPU time per group applied to the {W}x{H}x{F} "
+                       f"video's groups at {2 * cb['cores']} tiles, spread evenly over the cores")
+    cfg["timed_sample"] = {"W": sw, "H": sh, "frames": sf, "tiles": 2 * cb["cores"]}
+    cfg["tiles"] = 2 * cb["cores"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": config(args), "cpu_baseline": cb,
+            "data": "synthetic", "config": cfg, "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0

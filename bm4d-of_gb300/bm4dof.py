@@ -13,6 +13,7 @@ this module fails loudly when libbm4dof_gpu.so has not been built.
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 
 import numpy as np
@@ -605,9 +606,10 @@ class Trainer:
         _check(load().bm4dof_trainer_state(self._h, C.c_void_p(m1.ctypes.data), C.c_void_p(m2.ctypes.data),
                                            m1.size, C.byref(n), 1))
 
-    def checkpoint(self, path):
-        """Parameters and AdamW state to a host file (save_checkpoint)."""
-        save_checkpoint(path, self.params(), *self.state(), batch=self.batch)
+    def checkpoint(self, path, meta=None, best=None):
+        """Parameters and AdamW state to a host file (save_checkpoint), with
+        the caller's run record and best-epoch parameters when given."""
+        save_checkpoint(path, self.params(), *self.state(), batch=self.batch, meta=meta, best=best)
 
     def restore(self, path):
         """Parameters and AdamW state from a file written by checkpoint: the
@@ -615,6 +617,7 @@ class Trainer:
         ck = load_checkpoint(path)
         self.set_params(ck["params"])
         self.set_state(ck["moment1"], ck["moment2"], ck["steps"])
+        return ck
 
     def grad(self, feat, target):
         g = np.zeros(GAIN_PARAMS, np.float32)
@@ -639,27 +642,48 @@ class Trainer:
         return out
 
 
-CHECKPOINT_VERSION = 1
+CHECKPOINT_VERSION = 2
 
 
-def save_checkpoint(path, params, moment1, moment2, steps, batch=0):
+def save_checkpoint(path, params, moment1, moment2, steps, batch=0, meta=None, best=None):
     """Gain-network training checkpoint: FP32 parameters, AdamW moments (laid
-    out like the parameters) and step count in one .npz file."""
+    out like the parameters) and step count in one .npz file, optionally with
+    the training run's record (meta: a JSON-serialisable dict) and the
+    parameters of its best epoch.  The file is written beside its final name
+    and renamed over it, so a reader finds either the previous checkpoint or
+    this one, never a mixture or a partial file."""
     arrs = [np.ascontiguousarray(a, np.float32).ravel() for a in (params, moment1, moment2)]
+    if best is not None:
+        arrs.append(np.ascontiguousarray(best, np.float32).ravel())
     if any(a.size != GAIN_PARAMS for a in arrs):
         raise ValueError(f"checkpoint blobs hold {GAIN_PARAMS} floats each")
-    with open(path, "wb") as f:
+    extra = {}
+    if meta is not None:
+        extra["meta"] = np.array(json.dumps(meta))
+    if best is not None:
+        extra["best"] = arrs[3]
+    path = os.fspath(path)
+    tmp = path + ".tmp"
+    with open(tmp, "wb") as f:
         np.savez(f, version=np.array(CHECKPOINT_VERSION), params=arrs[0], moment1=arrs[1], moment2=arrs[2],
-                 steps=np.array(int(steps), np.uint64), batch=np.array(int(batch), np.uint64))
+                 steps=np.array(int(steps), np.uint64), batch=np.array(int(batch), np.uint64), **extra)
+        f.flush()
+        os.fsync(f.fileno())
+    os.replace(tmp, path)
 
 
 def load_checkpoint(path):
+    """A checkpoint as a dict: params, moment1, moment2, steps, batch, and
+    meta / best (None when the file holds none)."""
     with np.load(path) as z:
         if int(z["version"]) != CHECKPOINT_VERSION:
             raise ValueError(f"{path}: checkpoint version {int(z['version'])}, expected {CHECKPOINT_VERSION}")
         ck = {k: z[k].copy() for k in ("params", "moment1", "moment2")}
         ck["steps"], ck["batch"] = int(z["steps"]), int(z["batch"])
-    if any(ck[k].size != GAIN_PARAMS for k in ("params", "moment1", "moment2")):
+        ck["meta"] = json.loads(str(z["meta"])) if "meta" in z.files else None
+        ck["best"] = z["best"].copy() if "best" in z.files else None
+    if any(ck[k].size != GAIN_PARAMS for k in ("params", "moment1", "moment2")) or \
+            (ck["best"] is not None and ck["best"].size != GAIN_PARAMS):
         raise ValueError(f"{path}: checkpoint blobs hold {GAIN_PARAMS} floats each")
     return ck
 

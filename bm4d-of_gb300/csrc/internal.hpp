@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "../../include/bm4dof.h"
 
 namespace bm4dof {
 
@@ -22,6 +23,22 @@ bool make_basis(int transform, unsigned px, unsigned pt, std::vector<float> &bas
                 std::vector<float> &binv);
 // Aggregation window (src/core/nldct.cpp:698-737).
 std::vector<float> make_window(bool agg, unsigned px, unsigned pt);
+
+// Tiles of a run (subDivideTight, lib_videot.hpp:853-916) and the reference
+// grid of each (processNlBayes, nldct.cpp:520-553); runtime.cu.
+struct Plan {
+	int nW, nH, wTmp, hTmp;
+	std::vector<Tile> tiles;
+	std::vector<int> grid;     // per tile: [xs | inverse x] [ys | inverse y] [fs | inverse t]
+	long long G = 0;
+	size_t pix = 0;            // total tile pixels (one channel)
+	size_t maxpos = 0;         // largest tile pixel count
+};
+void determine_factor(unsigned n, unsigned &a, unsigned &b);
+// borders: null for the tiles of a run, else the six sides {x0, y0, t0, x1,
+// y1, t1} of one crop (bm4dof_process) that stop short of its source.
+void make_plan(Plan &pl, unsigned W, unsigned H, unsigned F, unsigned nparts, const bm4dof_params &p,
+               const int *borders);
 
 // search.cu
 int search_frames_max(const StepParams &sp);

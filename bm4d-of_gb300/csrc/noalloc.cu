@@ -46,23 +46,32 @@ void *g_scratch_addr[kMaxDevices];   // device address of g_search_scratch, per 
 
 size_t align256(size_t n) { return (n + 255) / 256 * 256; }
 
-// Grid positions along one axis (nldct.cpp:528-553): start, start+step, ...
-// below end, plus end-1 when the crop touches the image border there.
+// Grid positions along one axis (nldct.cpp:528-553) in closed form: `base`
+// positions ori, ori+step, ..., then, when `extra`, the last position before
+// the end of the crop (taken when the crop touches the image border there).
+// The setup kernel rebuilds the planner's list and its inverse from it.
 struct Axis {
-	int ori, end, step, extra, n;
+	int ori, step, base, extra, last, n;
 };
 
-Axis axis(int ori, int end, int step, bool last_forced)
+// The closed form of one of the planner's grid lists (make_plan, shared with
+// bm4dof_run); false when the list is not of that form, so that the device
+// copy can never differ from the planner's.
+bool axis_of(const int *list, int n, int step, Axis &a)
 {
-	Axis a;
-	a.ori = ori;
-	a.end = end;
+	a.ori = n > 0 ? list[0] : 0;
 	a.step = step;
-	const int span = end - ori;
-	const int base = span > 0 ? (span + step - 1) / step : 0;
-	a.extra = (span > 0 && last_forced && (span - 1) % step != 0) ? 1 : 0;
-	a.n = base + a.extra;
-	return a;
+	a.n = n;
+	a.base = n;
+	a.extra = 0;
+	a.last = n > 0 ? list[n - 1] : 0;
+	if (n >= 2 && (list[n - 1] - a.ori) % step != 0) {
+		a.extra = 1;
+		a.base = n - 1;
+	}
+	for (int i = 0; i < a.base; i++)
+		if (list[i] != a.ori + i * step) return false;
+	return !a.extra || list[n - 1] > list[n - 2];
 }
 
 // Writes the tile descriptor and the grid lists (with their inverse maps,
@@ -78,11 +87,11 @@ __global__ void setup_kernel(Tile T, Axis ax, Axis ay, Axis af, int F, Tile *til
 		int *list = grid + offs[k];
 		int *inv = list + a.n;
 		for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
-			list[i] = (a.extra && i == a.n - 1) ? a.end - 1 : a.ori + i * a.step;
+			list[i] = i < a.base ? a.ori + i * a.step : a.last;
 		for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < ext[k]; x += gridDim.x * blockDim.x) {
 			int v = -1;
-			if (x >= a.ori && x < a.end && (x - a.ori) % a.step == 0) v = (x - a.ori) / a.step;
-			else if (a.extra && x == a.end - 1) v = a.n - 1;
+			if (x >= a.ori && (x - a.ori) % a.step == 0 && (x - a.ori) / a.step < a.base) v = (x - a.ori) / a.step;
+			else if (a.extra && x == a.last) v = a.n - 1;
 			inv[x] = v;
 		}
 	}
@@ -162,39 +171,22 @@ extern "C" bm4dof_status bm4dof_search_groups_noalloc(const float *video, const 
 	}
 
 	// the tile (subDivideTight, lib_videot.hpp:853-916) and its grid
-	// (processNlBayes, nldct.cpp:520-553)
-	unsigned nW = 1, nH = 1;
-	if (nparts > 1) {
-		nH = 2;
-		while (nparts % nH > 0) nH++;
-		nW = nparts / nH;
-		if (nH > nW) { nW = nH; nH = nparts / nW; }
-	}
-	if (tile >= nW * nH) return fail(BM4DOF_ERR_ARGUMENT, "bm4dof_search_groups_noalloc: tile out of range");
-	const int wTmp = (int)std::ceil(float(W) / float(nW)), hTmp = (int)std::ceil(float(H) / float(nH));
-	const int q = (int)(tile % nW), pp = (int)(tile / nW), N = (int)p->boundary;
-	Tile T = {};
-	T.ox = std::max(0, q * wTmp - N);
-	T.oy = std::max(0, pp * hTmp - N);
-	const int ex = std::min((int)W, (q + 1) * wTmp + N), ey = std::min((int)H, (pp + 1) * hTmp + N);
-	T.w = ex - T.ox;
-	T.h = ey - T.oy;
-	T.bx0 = T.ox > 0;
-	T.by0 = T.oy > 0;
-	T.bx1 = ex < (int)W;
-	T.by1 = ey < (int)H;
-	const int sWx = (int)p->sizeSearchWindow;
-	const Axis ax = axis(T.bx0 ? (int)px - 1 + sWx / 2 : 0, T.w - (T.bx1 ? (int)px - 1 + sWx / 2 : (int)px - 1),
-	                     (int)p->offSet, !T.bx1);
-	const Axis ay = axis(T.by0 ? (int)px - 1 + sWx / 2 : 0, T.h - (T.by1 ? (int)px - 1 + sWx / 2 : (int)px - 1),
-	                     (int)p->offSet, !T.by1);
-	const Axis af = axis(0, (int)F - ((int)pt - 1), (int)p->offSetTime, true);
-	T.nx = ax.n;
-	T.ny = ay.n;
-	T.nf = af.n;
+	// (processNlBayes, nldct.cpp:520-553), from the planner bm4dof_run uses
+	Plan pl;
+	make_plan(pl, W, H, F, nparts, *p, nullptr);
+	if (tile >= pl.tiles.size()) return fail(BM4DOF_ERR_ARGUMENT, "bm4dof_search_groups_noalloc: tile out of range");
+	Tile T = pl.tiles[tile];
+	Axis ax, ay, af;
+	if (!axis_of(&pl.grid[T.gx], T.nx, (int)p->offSet, ax) || !axis_of(&pl.grid[T.gy], T.ny, (int)p->offSet, ay) ||
+	    !axis_of(&pl.grid[T.gf], T.nf, (int)p->offSetTime, af))
+		return fail(BM4DOF_ERR_UNSUPPORTED, "bm4dof_search_groups_noalloc: reference grid without a closed form");
 	T.gx = 0;
 	T.gy = T.gx + T.nx + T.w;
 	T.gf = T.gy + T.ny + T.h;
+	T.g0 = 0;
+	T.pix0 = 0;
+	T.lin0 = 0;
+	const int sWx = (int)p->sizeSearchWindow;
 	const long long G = (long long)T.nx * T.ny * T.nf;
 	*count = (size_t)G;
 
@@ -220,8 +212,7 @@ extern "C" bm4dof_status bm4dof_search_groups_noalloc(const float *video, const 
 	const size_t grid_ints = (size_t)T.nx + T.w + T.ny + T.h + T.nf + F;
 	const size_t o_tile = 0;
 	const size_t o_grid = o_tile + align256(sizeof(Tile));
-	const size_t o_err = o_grid + align256(grid_ints * sizeof(int));
-	const size_t o_traj = o_err + 256;
+	const size_t o_traj = o_grid + align256(grid_ints * sizeof(int));
 	const size_t o_nsimp = o_traj + align256((size_t)G * nfm * sizeof(uint32_t));
 	const size_t o_idx = o_nsimp + align256((size_t)G);
 	const size_t need = o_idx + align256((size_t)G * np * sizeof(uint32_t));
@@ -229,13 +220,15 @@ extern "C" bm4dof_status bm4dof_search_groups_noalloc(const float *video, const 
 		return fail(BM4DOF_ERR_ARGUMENT, "bm4dof_search_groups_noalloc: this tile needs " + std::to_string(need) +
 		                                     " bytes of scratch; the static scratch holds " +
 		                                     std::to_string(kScratchBytes) + " (" + std::to_string(G) + " groups)");
-	if (G > 0 && cap > 0 && (!ref || !nsimp || !index || stride == 0))
+	// a size query (cap = 0) stops here: it launches nothing and leaves the
+	// scratch alone
+	if (cap == 0 || G == 0) return BM4DOF_OK;
+	if (!ref || !nsimp || !index || stride == 0)
 		return fail(BM4DOF_ERR_ARGUMENT, "bm4dof_search_groups_noalloc: null output array");
 
 	unsigned char *s = static_cast<unsigned char *>(base);
 	Tile *d_tile = reinterpret_cast<Tile *>(s + o_tile);
 	int *d_grid = reinterpret_cast<int *>(s + o_grid);
-	int *d_err = reinterpret_cast<int *>(s + o_err);
 	uint32_t *d_traj = reinterpret_cast<uint32_t *>(s + o_traj);
 	uint8_t *d_nsimp = s + o_nsimp;
 	uint32_t *d_idx = reinterpret_cast<uint32_t *>(s + o_idx);
@@ -244,8 +237,6 @@ extern "C" bm4dof_status bm4dof_search_groups_noalloc(const float *video, const 
 	int nsm = 0;
 	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
 	setup_kernel<<<8, 256, 0, st>>>(T, ax, ay, af, (int)F, d_tile, d_grid);
-	e = cudaMemsetAsync(d_err, 0, sizeof(int), st);   // starts at zero on every call
-	if (e != cudaSuccess) return fail(BM4DOF_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
 	Image src;
 	src.p = const_cast<float *>(video);
 	src.W = (int)W;
@@ -258,14 +249,12 @@ extern "C" bm4dof_status bm4dof_search_groups_noalloc(const float *video, const 
 	ff.p = const_cast<float *>(fflow);
 	bf.p = const_cast<float *>(bflow);
 	if ((e = launch_traj(ff, bf, d_tile, 1, d_grid, sp, G, d_traj, st)) != cudaSuccess ||
-	    (e = launch_search(src, d_tile, 1, d_grid, d_traj, sp, 0, G, d_nsimp, d_idx, d_err, nsm, st)) != cudaSuccess)
+	    (e = launch_search(src, d_tile, 1, d_grid, d_traj, sp, 0, G, d_nsimp, d_idx, nullptr, nsm, st)) != cudaSuccess)
 		return fail(BM4DOF_ERR_CUDA, std::string("search launch: ") + cudaGetErrorString(e));
 	const long long nout = std::min<long long>(G, (long long)cap);
-	if (nout > 0) {
-		const long long b = std::min<long long>((nout + 255) / 256, 4096);
-		export_kernel<<<(int)b, 256, 0, st>>>(T, (int)C, (int)np, nout, d_grid, d_nsimp, d_idx, ref, nsimp, index,
-		                                      stride);
-	}
+	const long long b = std::min<long long>((nout + 255) / 256, 4096);
+	export_kernel<<<(int)b, 256, 0, st>>>(T, (int)C, (int)np, nout, d_grid, d_nsimp, d_idx, ref, nsimp, index,
+	                                      stride);
 	if ((e = cudaGetLastError()) != cudaSuccess)
 		return fail(BM4DOF_ERR_CUDA, std::string("export launch: ") + cudaGetErrorString(e));
 	return BM4DOF_OK;

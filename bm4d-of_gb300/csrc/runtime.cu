@@ -158,6 +158,10 @@ struct Mark {
 	}
 };
 
+}  // namespace
+
+namespace bm4dof {
+
 void determine_factor(unsigned n, unsigned &a, unsigned &b)
 {
 	// utilities.cpp:137-158: n = a*b with a >= b as balanced as possible
@@ -167,15 +171,6 @@ void determine_factor(unsigned n, unsigned &a, unsigned &b)
 	a = n / b;
 	if (b > a) { a = b; b = n / a; }
 }
-
-struct Plan {
-	int nW, nH, wTmp, hTmp;
-	std::vector<Tile> tiles;
-	std::vector<int> grid;     // per tile: [xs | inverse x] [ys | inverse y] [fs | inverse t]
-	long long G = 0;
-	size_t pix = 0;            // total tile pixels (one channel)
-	size_t maxpos = 0;         // largest tile pixel count
-};
 
 // Tiles (subDivideTight, lib_videot.hpp:853-916) and their reference grids
 // (processNlBayes, nldct.cpp:520-553).  With borders (bm4dof_process) the plan
@@ -263,6 +258,10 @@ void make_plan(Plan &pl, unsigned W, unsigned H, unsigned F, unsigned nparts, co
 			pl.tiles.push_back(T);
 		}
 }
+
+}  // namespace bm4dof
+
+namespace {
 
 // The crop's sides that stop short of its source (nldct.cpp:520-525), in
 // make_plan's order {x0, y0, t0, x1, y1, t1}; no crop: no border.
@@ -404,13 +403,17 @@ bm4dof_status hbuf(bm4dof_ctx *ctx, const std::string &name, size_t bytes, unsig
 	return BM4DOF_OK;
 }
 
-// Bytes of aggregation terms per chunk: 16 GB, BM4DOF_SLOT_MB when set, at
-// most half of the device memory this context could use.
+// Bytes of aggregation terms per chunk: 16 GB, BM4DOF_SLOT_MB when set (a
+// decimal number of MiB, fractions allowed), at most half of the device
+// memory this context could use.
 void set_budget(bm4dof_ctx *ctx)
 {
 	if (ctx->fixed_budget) return;
 	size_t budget = (size_t)16384 << 20;
-	if (const char *env = std::getenv("BM4DOF_SLOT_MB")) budget = (size_t)std::atoll(env) << 20;
+	if (const char *env = std::getenv("BM4DOF_SLOT_MB")) {
+		const double mb = std::atof(env);
+		if (mb > 0.0) budget = (size_t)(mb * 1048576.0);
+	}
 	size_t freeb = 0, totalb = 0;
 	if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess && budget > (freeb + ctx->held) / 2)
 		budget = (freeb + ctx->held) / 2;

@@ -15,11 +15,13 @@ backward and AdamW kernels (bm4dof_trainer_*), cosine learning-rate decay, and
 saved as a float32 blob (BM4DOF_GAIN_PARAMS values, bm4dof.split_params
 layout) in an .npz together with its training record.
 
-With --checkpoint the trainer's parameters and AdamW state are written to
-FILE after every epoch (Trainer.checkpoint), with the epoch count and the best
-validation epoch beside it in FILE.json; --resume restores them and continues
-with the next epoch (the shuffles of the finished epochs are replayed, so the
-run takes the steps an uninterrupted one would have taken).
+With --checkpoint the trainer's parameters and AdamW state, the epoch count,
+the losses so far and the best validation epoch's parameters are written to
+FILE after every epoch, as one file renamed into place (Trainer.checkpoint);
+--resume restores them and continues with the next epoch (the shuffles of the
+finished epochs are replayed, so the run takes the steps an uninterrupted one
+would have taken).  It refuses a checkpoint of a run with other data, batch,
+seed or epoch count.
 
 The last 5 % of the clips are held out for the validation loss.  The record
 also holds PSNR on a held-out 256x256x12 clip at sigma 20: plain method,
@@ -101,24 +103,34 @@ def evaluate(ctx, params, W=256, H=256, F=12, sigma=20.0, seed=424242, kappa=0.0
 def train(feat, tgt, epochs, batch, lr, wd, seed, val=None, log=print, checkpoint=None, resume=False):
     """AdamW with cosine decay; returns the trainer holding the parameters of
     the epoch with the lowest validation loss (the last epoch without val).
-    checkpoint: file written after every epoch; resume: continue from it."""
+    checkpoint: file written after every epoch (trainer state, run record and
+    best-epoch parameters in one atomically replaced file); resume: continue
+    from it.  A checkpoint of another run (other sample count, batch, seed or
+    epoch count) or one whose AdamW step count disagrees with its epoch count
+    is refused."""
     import torch
     tr = bm4dof.Trainer(batch=batch, seed=seed)
     n = feat.shape[0]
     gen = torch.Generator().manual_seed(seed)
     per_epoch = max(1, n // batch)
     total = epochs * per_epoch
+    run = {"samples": int(n), "batch": int(batch), "seed": int(seed), "epochs": int(epochs),
+           "per_epoch": int(per_epoch)}
     step = 0
     history, vhist = [], []
     best = (float("inf"), None)
     start = 0
     if checkpoint and resume and os.path.exists(checkpoint):
-        tr.restore(checkpoint)
-        with open(checkpoint + ".json") as f:
-            meta = json.load(f)
+        ck = tr.restore(checkpoint)
+        meta = ck["meta"]
+        if meta is None or meta.get("run") != run:
+            raise ValueError(f"{checkpoint}: written by another training run "
+                             f"({None if meta is None else meta.get('run')} vs {run})")
         start, history, vhist = meta["epochs_done"], meta["train_loss"], meta["val_loss_per_epoch"]
+        if ck["steps"] != start * per_epoch:
+            raise ValueError(f"{checkpoint}: {ck['steps']} AdamW steps after {start} epochs of {per_epoch}")
         if meta.get("best_val") is not None:
-            best = (meta["best_val"], bm4dof.load_checkpoint(checkpoint + ".best.npz")["params"])
+            best = (meta["best_val"], ck["best"])
         step = start * per_epoch
         for _ in range(start):
             torch.randperm(n, generator=gen)     # the shuffles of the finished epochs
@@ -142,14 +154,12 @@ def train(feat, tgt, epochs, batch, lr, wd, seed, val=None, log=print, checkpoin
             msg += f"  validation {vl:.5f}"
             if vl < best[0]:
                 best = (vl, tr.params())
-                if checkpoint:
-                    bm4dof.save_checkpoint(checkpoint + ".best.npz", best[1], *tr.state())
-        log(msg)
         if checkpoint:
-            tr.checkpoint(checkpoint)
-            with open(checkpoint + ".json", "w") as f:
-                json.dump({"epochs_done": e + 1, "train_loss": history, "val_loss_per_epoch": vhist,
-                           "best_val": None if best[1] is None else best[0]}, f)
+            tr.checkpoint(checkpoint, meta={"run": run, "epochs_done": e + 1, "train_loss": history,
+                                            "val_loss_per_epoch": vhist,
+                                            "best_val": None if best[1] is None else best[0]},
+                          best=best[1])
+        log(msg)
     if best[1] is not None:
         tr.set_params(best[1])
     return tr, history, vhist

@@ -226,8 +226,12 @@ bm4dof_status bm4dof_get_groups(bm4dof_ctx *ctx, unsigned step, unsigned tile,
  * Outputs, in processing order, for every grid group of tile `tile` of
  * `nparts` tiles: ref[g], nsimp[g] and index[g*stride + n] in the format of
  * bm4dof_get_groups (at most cap groups are written; *count = total).  The
- * mask switch-offs of bm4dof_run are not applied, and the search is the
- * reference's default (exhaustive) one.  The first call on a device
+ * tiles and grids are those of bm4dof_run.  Unlike bm4dof_get_groups, every
+ * grid group is returned: the mask switch-offs of bm4dof_run are not applied
+ * (a group that bm4dof_run skips still appears here), and the search is the
+ * reference's default (exhaustive) one.  A size query (cap = 0) only sets
+ * *count: it launches nothing and does not touch the scratch.  The first call
+ * on a device
  * looks up the scratch's device address, so make it before any stream
  * capture.  Asynchronous on `stream` (a cudaStream_t, NULL for the default
  * stream); calls that overlap on the GPU share the scratch and race. */

@@ -37,6 +37,9 @@
 #include <string>
 #include <thread>
 #include <vector>
+#if defined(__linux__)
+#include <sched.h>
+#endif
 
 #include "bm4dof.h"
 
@@ -159,11 +162,21 @@ void printNlbParameters(const Params &params)
 
 /* ---- the run ------------------------------------------------------------- */
 
-/* 2 x the reference's OpenMP thread count (see the header comment). */
+/* 2 x the reference's OpenMP thread count (see the header comment).  Without
+ * OMP_NUM_THREADS, libgomp starts one thread per CPU the process may run on
+ * (its affinity mask, which taskset or a cpuset narrows), not one per online
+ * CPU. */
 inline unsigned default_tiles()
 {
 	const char *e = std::getenv("OMP_NUM_THREADS");
 	long t = e ? std::strtol(e, nullptr, 10) : 0;
+#if defined(__linux__)
+	if (t <= 0) {
+		cpu_set_t set;
+		CPU_ZERO(&set);
+		if (sched_getaffinity(0, sizeof(set), &set) == 0) t = CPU_COUNT(&set);
+	}
+#endif
 	if (t <= 0) t = (long)std::thread::hardware_concurrency();
 	return 2u * (unsigned)(t > 0 ? t : 1);
 }

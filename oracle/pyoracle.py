@@ -17,7 +17,6 @@ ORACLE_SO = os.path.join(HERE, "libbm4dof_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libbm4dof_ref.so")
 # the reference built with its VBM3D_SEARCH switch (predictive patch search)
 REF_VBM3D_SO = os.path.join(HERE, "_ref", "libbm4dof_ref_vbm3d.so")
-REF_ROOT_DEFAULT = "/root/reference"
 VBM3D_SEARCH = 0x10   # BM4DOF_VBM3D_SEARCH of include/bm4dof.h
 
 
@@ -85,11 +84,19 @@ def _fp(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
 
 
-def build(ref_root: str | None = None) -> None:
-    """Compile the oracle, and the reference when its sources are present."""
+def ref_root() -> str | None:
+    """The reference's source tree: the REF_ROOT environment variable (no
+    default), or None when it is unset or holds no reference sources."""
+    root = os.environ.get("REF_ROOT")
+    return root if root and os.path.isfile(os.path.join(root, "src", "core", "nldct.cpp")) else None
+
+
+def build(ref_root_dir: str | None = None) -> None:
+    """Compile the oracle, and the reference when its source tree is given
+    (argument or REF_ROOT)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    root = ref_root or REF_ROOT_DEFAULT
-    if os.path.isfile(os.path.join(root, "src", "core", "nldct.cpp")):
+    root = ref_root_dir or ref_root()
+    if root and os.path.isfile(os.path.join(root, "src", "core", "nldct.cpp")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={root}"], check=True)
 
 

@@ -23,6 +23,9 @@ CASES = [
     ("video_paste_4tiles", 44, 40, 6, 1, 20.0, 24, True, dict(CFG_VIDEO, paste_boost=True), 2),
     ("image_paste", 48, 40, 1, 1, 20.0, 25, False, dict(CFG_IMAGE, paste_boost=True), 1),
     ("rgb_video_paste", 30, 28, 4, 3, 20.0, 26, True, dict(CFG_VIDEO, paste_boost=True), 1),
+    # the plain two-step method on one 256x256 grey image: 8x8 patches, bior1.5
+    # in step 1, Kaiser aggregation window (nldct.cpp:637-714), 2 tiles
+    ("config1_image", 256, 256, 1, 1, 20.0, 1, False, CFG_IMAGE, 1),
 ]
 
 # The reference built with its VBM3D_SEARCH switch: predictive search (the

@@ -48,7 +48,9 @@ def layer(gpulib, tmp_path_factory):
 @pytest.fixture(scope="module")
 def layer_ref(gpulib, reference, tmp_path_factory):
     import pyoracle
-    root = pyoracle.REF_ROOT_DEFAULT
+    root = pyoracle.ref_root()
+    if root is None:
+        pytest.skip("REF_ROOT (the reference's source tree) not set")
     inc = ["-fopenmp", "-I" + os.path.join(ORACLE, "ref_stubs"), "-I" + os.path.join(root, "src", "core"),
            "-I" + os.path.join(root, "src", "utils"), "-DWITH_REFERENCE_TYPES"]
     libs = [pyoracle.REF_SO, "-Wl,-rpath," + os.path.dirname(pyoracle.REF_SO)]
@@ -142,14 +144,21 @@ def test_gpu_layer_run_equals_the_library(layer, gpulib, gpuctx, tmp_path):
 
 def test_layer_tile_count_follows_openmp(layer):
     # 2 x omp_get_max_threads() as the reference (nldct.cpp:318-323): from
-    # OMP_NUM_THREADS when set, else the host's hardware threads
+    # OMP_NUM_THREADS when set, else the CPUs the process may run on (libgomp
+    # counts its affinity mask, not the online CPUs)
     env = {k: v for k, v in os.environ.items() if k != "OMP_NUM_THREADS"}
     r = subprocess.run([layer, "tiles"], capture_output=True, text=True, env=dict(env, OMP_NUM_THREADS="3"))
     assert r.stdout.strip() == "6"
     r = subprocess.run([layer, "tiles"], capture_output=True, text=True, env=dict(env, OMP_NUM_THREADS="4,2"))
     assert r.stdout.strip() == "8"
     r = subprocess.run([layer, "tiles"], capture_output=True, text=True, env=env)
-    assert r.stdout.strip() == str(2 * (os.cpu_count() or 1))
+    assert r.stdout.strip() == str(2 * len(os.sched_getaffinity(0)))
+    taskset = shutil.which("taskset")
+    if taskset:
+        cpu = sorted(os.sched_getaffinity(0))[0]
+        r = subprocess.run([taskset, "-c", str(cpu), layer, "tiles"], capture_output=True, text=True, env=env)
+        assert r.returncode == 0, r.stderr
+        assert r.stdout.strip() == "2"
 
 
 def test_layer_process_refuses_sizes_it_cannot_read(layer):
