@@ -44,9 +44,12 @@ void make_plan(Plan &pl, unsigned W, unsigned H, unsigned F, unsigned nparts, co
 int search_frames_max(const StepParams &sp);
 cudaError_t launch_traj(const Image &ffl, const Image &bfl, const Tile *tiles, int ntiles, const int *grid,
                         const StepParams &sp, long long G, uint32_t *traj, cudaStream_t st);
+// With glist, the groups glist[0 .. *gcount) (a device-side count, at most
+// g_end - g_begin of them) instead of the range [g_begin, g_end).
 cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const int *grid,
                           const uint32_t *traj, const StepParams &sp, long long g_begin, long long g_end,
-                          uint8_t *nsimp, uint32_t *idx, int *err, int nsm, cudaStream_t st);
+                          uint8_t *nsimp, uint32_t *idx, int *err, int nsm, cudaStream_t st,
+                          const uint32_t *glist = nullptr, const unsigned *gcount = nullptr);
 
 // search_vbm3d.cu (the reference's VBM3D_SEARCH build)
 bool vbm3d_check(const StepParams &sp, const std::vector<Tile> &tiles, std::string &why);
@@ -61,6 +64,17 @@ bool mixed_supported(const StepParams &sp);
 cudaError_t launch_search_mixed(const Image &src, const Tile *tiles, int ntiles, const int *grid,
                                 const uint32_t *traj, const StepParams &sp, const long long *blocks,
                                 long long nblocks, uint8_t *nsimp, uint32_t *idx, int nsm, cudaStream_t st);
+
+// search_tc.cu: tensor-core pre-screen + certified exact re-rank; the groups
+// it cannot certify are listed for launch_search (list mode)
+void tc_blocks(const std::vector<Tile> &tiles, std::vector<long long> &out);
+bool tc_supported(const StepParams &sp, const std::vector<Tile> &tiles);
+size_t tc_smem_bytes();
+cudaError_t launch_search_tc(const Image &src, const Tile *tiles, int ntiles, const int *grid, const uint32_t *traj,
+                             const StepParams &sp, const long long *blocks, long long nblocks, long long G,
+                             uint32_t *cand, float *lb, int *status, uint8_t *nsimp, uint32_t *idx,
+                             uint32_t *fallback, unsigned *nfallback, int nsm, cudaStream_t st);
+cudaError_t tc_selftest(const uint16_t *A, const uint16_t *B, float *D, int *status, cudaStream_t st);
 
 // filter.cu
 size_t filter_smem_bytes(const StepParams &sp);

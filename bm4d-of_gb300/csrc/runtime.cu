@@ -58,6 +58,9 @@ struct bm4dof_ctx {
 	bool has_gain = false;
 	float kappa = 1.5f;
 	unsigned long long l_groups = 0, l_fallbacks = 0;
+	// mixed form: groups searched through the tensor-core pre-screen, and the
+	// ones it left to the exact search, over both steps of the last run
+	unsigned long long m_groups = 0, m_exact = 0;
 	size_t slot_budget = 0;   // bytes of per-chunk aggregation terms
 	bool fixed_budget = false;   // batched children: slot_budget set by the tuning
 	bool no_marks = false;       // inside a graph capture: no timing events
@@ -345,7 +348,8 @@ struct StepState {
 	Plan pl;
 	StepParams sp;
 	long long G = 0, chunk = 0;
-	bool mixed_search = false;
+	bool mixed_search = false;   // FP16 mma.sync pre-screen (search_mixed.cu)
+	bool tc_search = false;      // tcgen05 pre-screen + certified re-rank (search_tc.cu)
 	size_t nblocks = 0;
 	PasteScratch paste = {nullptr, nullptr, nullptr, nullptr, nullptr};   // doPasteBoost only
 	Tile *d_tiles = nullptr;
@@ -353,8 +357,11 @@ struct StepState {
 	float *d_basis = nullptr, *d_binv = nullptr, *d_win = nullptr;
 	uint8_t *d_nsimp = nullptr, *d_alive = nullptr, *d_eq = nullptr, *d_killed = nullptr;
 	uint32_t *d_idx = nullptr, *d_traj = nullptr;
+	uint32_t *d_cand = nullptr, *d_fb = nullptr;   // tc_search: candidates, exact-search list
+	float *d_lb = nullptr;                          // tc_search: bound on the dropped candidates
 	float *d_wgroup = nullptr;
-	unsigned *d_small = nullptr;          // [0] edges, [3] fallbacks, [64..] per-tile counts
+	unsigned *d_small = nullptr;          // [0] edges, [3] fallbacks, [4] exact-search list, [5] tc status,
+	                                      // [64..] per-tile counts
 	long long *d_blocks = nullptr;
 	unsigned long long *d_edges = nullptr;
 	float *d_acc = nullptr, *d_wacc = nullptr, *d_vals = nullptr;
@@ -491,9 +498,11 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 		return BM4DOF_ERR_BIOR_SIZE;
 	}
 	std::vector<float> win = make_window(p.agg_window != 0, sp.px, sp.pt);
-	S.mixed_search = mode.mixed && mixed_supported(sp);
+	S.tc_search = mode.mixed && tc_supported(sp, pl.tiles);
+	S.mixed_search = mode.mixed && !S.tc_search && mixed_supported(sp);
 	std::vector<long long> blocks;
-	if (S.mixed_search) mixed_blocks(pl.tiles, blocks);
+	if (S.tc_search) tc_blocks(pl.tiles, blocks);
+	else if (S.mixed_search) mixed_blocks(pl.tiles, blocks);
 	S.nblocks = blocks.size();
 
 	// host staging
@@ -534,7 +543,12 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	SBUF("small", 64 + ntiles, S.d_small);
 	SBUF("traj", (size_t)G * search_frames_max(sp), S.d_traj);
 	SBUF("edges", G, S.d_edges);   // a group switches off at most one other
-	if (S.mixed_search) SBUF("mixed_blocks", blocks.size(), S.d_blocks);
+	if (S.mixed_search || S.tc_search) SBUF("mixed_blocks", blocks.size(), S.d_blocks);
+	if (S.tc_search) {
+		SBUF("tc_cand", (size_t)G * 32, S.d_cand);
+		SBUF("tc_lb", G, S.d_lb);
+		SBUF("tc_exact", G, S.d_fb);
+	}
 	if (sp.paste) {
 		SBUF("paste_pending", G, S.paste.pending);
 		SBUF("paste_state", G, S.paste.state);
@@ -599,7 +613,7 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 		CK(cudaMemcpyAsync(S.d_basis, S.h_stage + S.o_basis, nbasis, cudaMemcpyHostToDevice, st));
 		CK(cudaMemcpyAsync(S.d_binv, S.h_stage + S.o_binv, nbasis, cudaMemcpyHostToDevice, st));
 		CK(cudaMemcpyAsync(S.d_win, S.h_stage + S.o_win, sizeof(float) * sp.spc, cudaMemcpyHostToDevice, st));
-		if (S.mixed_search)
+		if (S.mixed_search || S.tc_search)
 			CK(cudaMemcpyAsync(S.d_blocks, S.h_stage + S.o_blocks, sizeof(long long) * S.nblocks,
 			                   cudaMemcpyHostToDevice, st));
 		CK(cudaMemsetAsync(S.d_small, 0, sizeof(unsigned) * (64 + ntiles), st));
@@ -613,6 +627,18 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 			CK(launch_search_vbm3d(on_noisy ? noisy : basic, ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp,
 			                       on_noisy ? 1 : (int)C, 0, G, S.d_nsimp, S.d_idx, ctx->nsm, st));
 			ctx->launches += 1;
+		} else if (S.tc_search) {
+			// tensor-core pre-screen and certified re-rank; the groups it cannot
+			// certify get the exact search
+			const Image &src = on_noisy ? noisy : basic;
+			CK(launch_traj(ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp, G, S.d_traj, st));
+			CK(cudaMemsetAsync(S.d_lb, 0xff, sizeof(float) * G, st));   // NaN: not certified
+			CK(launch_search_tc(src, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, S.d_blocks, (long long)S.nblocks, G,
+			                    S.d_cand, S.d_lb, reinterpret_cast<int *>(S.d_small + 5), S.d_nsimp, S.d_idx, S.d_fb,
+			                    S.d_small + 4, ctx->nsm, st));
+			CK(launch_search(src, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, 0, G, S.d_nsimp, S.d_idx, nullptr,
+			                 ctx->nsm, st, S.d_fb, S.d_small + 4));
+			ctx->launches += 4;
 		} else if (S.mixed_search) {
 			// FP16 tensor-core pre-screen + exact re-rank of the best 2k
 			CK(launch_traj(ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp, G, S.d_traj, st));
@@ -753,6 +779,10 @@ float step_ratio(bm4dof_ctx *ctx, int slot)
 	if (S.mode.learned) {
 		ctx->l_groups = groups;
 		ctx->l_fallbacks = S.h_small[3];
+	}
+	if (S.tc_search) {
+		ctx->m_groups += (unsigned long long)S.G;
+		ctx->m_exact += S.h_small[4];
 	}
 	return r;
 }
@@ -1063,6 +1093,7 @@ bm4dof_status launch_run(bm4dof_ctx *ctx, const RunArgs &r)
 bm4dof_status finish_run(bm4dof_ctx *ctx, const RunArgs &r, float ratios[2])
 {
 	float gr[2] = {0.f, 0.f};
+	ctx->m_groups = ctx->m_exact = 0;
 	if (r.run1) gr[0] = step_ratio(ctx, 0);
 	if (r.run2) gr[1] = step_ratio(ctx, 1);
 	if (r.keep) {
@@ -1560,6 +1591,43 @@ bm4dof_status bm4dof_learned_stats(bm4dof_ctx *ctx, unsigned long long *groups, 
 	if (!ctx) return BM4DOF_ERR_ARGUMENT;
 	if (groups) *groups = ctx->l_groups;
 	if (fallbacks) *fallbacks = ctx->l_fallbacks;
+	return BM4DOF_OK;
+}
+
+bm4dof_status bm4dof_mixed_stats(bm4dof_ctx *ctx, unsigned long long *groups, unsigned long long *exact)
+{
+	CtxLock lock_(ctx);
+	if (!ctx) return BM4DOF_ERR_ARGUMENT;
+	if (groups) *groups = ctx->m_groups;
+	if (exact) *exact = ctx->m_exact;
+	return BM4DOF_OK;
+}
+
+bm4dof_status bm4dof_tc_selftest(const void *a, const void *b, float *d, void *stream)
+{
+	clear_error();
+	if (!a || !b || !d) {
+		set_error("bm4dof_tc_selftest: null argument");
+		return BM4DOF_ERR_ARGUMENT;
+	}
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	int *status = nullptr;
+	cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&status), sizeof(int), st);
+	if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, sizeof(int), st);
+	if (e == cudaSuccess)
+		e = tc_selftest(static_cast<const uint16_t *>(a), static_cast<const uint16_t *>(b), d, status, st);
+	int h = 0;
+	if (e == cudaSuccess) e = cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+	if (status) cudaFreeAsync(status, st);
+	if (e != cudaSuccess) {
+		set_error(std::string("bm4dof_tc_selftest: ") + cudaGetErrorString(e));
+		return BM4DOF_ERR_CUDA;
+	}
+	if (h) {
+		set_error("bm4dof_tc_selftest: the MMA completion wait gave up");
+		return BM4DOF_ERR_CUDA;
+	}
 	return BM4DOF_OK;
 }
 

@@ -87,6 +87,8 @@ struct SearchArgs {
 	const uint32_t *traj;
 	int nfm;
 	long long g_begin, g_end;
+	const uint32_t *glist;   // when set: the groups glist[0 .. *gcount) instead of [g_begin, g_end)
+	const unsigned *gcount;
 	uint8_t *nsimp;
 	uint32_t *idx;
 };
@@ -290,7 +292,9 @@ search_kernel(Image src, StepParams sp, SearchArgs a)
 
 	const int tid = threadIdx.x;
 	const int chn = sp.chn_search;
-	for (long long g = a.g_begin + blockIdx.x; g < a.g_end; g += gridDim.x) {
+	const long long ng = a.glist ? (long long)*a.gcount : a.g_end - a.g_begin;
+	for (long long gi = blockIdx.x; gi < ng; gi += gridDim.x) {
+		const long long g = a.glist ? (long long)a.glist[gi] : a.g_begin + gi;
 		if (tid < 32) plan_group(a, sp, g, fw, s_nframes, s_ncand, s_nitems, s_tile, s_x, s_y, s_t);
 		__syncthreads();
 		const Tile T = a.tiles[s_tile];
@@ -398,10 +402,11 @@ cudaError_t launch_traj(const Image &ffl, const Image &bfl, const Tile *tiles, i
 
 cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const int *grid,
                           const uint32_t *traj, const StepParams &sp, long long g_begin, long long g_end,
-                          uint8_t *nsimp, uint32_t *idx, int *err, int nsm, cudaStream_t st)
+                          uint8_t *nsimp, uint32_t *idx, int *err, int nsm, cudaStream_t st, const uint32_t *glist,
+                          const unsigned *gcount)
 {
 	if (g_end <= g_begin) return cudaSuccess;
-	if (sp.np <= 1) {
+	if (sp.np <= 1 && !glist) {
 		const long long n = g_end - g_begin;
 		const int blocks = (int)((n + 255) / 256 < 65535 ? (n + 255) / 256 : 65535);
 		search_single_kernel<<<blocks, 256, 0, st>>>(tiles, ntiles, grid, sp, g_begin, g_end, nsimp, idx);
@@ -415,6 +420,8 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
 	a.nfm = search_frames_max(sp);
 	a.g_begin = g_begin;
 	a.g_end = g_end;
+	a.glist = glist;
+	a.gcount = gcount;
 	a.nsimp = nsimp;
 	a.idx = idx;
 	(void)err;

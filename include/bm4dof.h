@@ -348,6 +348,19 @@ bm4dof_status bm4dof_set_gain_network(bm4dof_ctx *ctx, const float *params, size
 bm4dof_status bm4dof_learned_stats(bm4dof_ctx *ctx, unsigned long long *groups,
                                    unsigned long long *fallbacks);
 
+/* No counterpart in the reference.  Groups whose patch search went through
+ * the tensor-core pre-screen in the last BM4DOF_MIXED_PRECISION run (both
+ * steps), and how many of them the certified re-rank left to the exact
+ * search.  Either way the neighbour lists are the exact search's. */
+bm4dof_status bm4dof_mixed_stats(bm4dof_ctx *ctx, unsigned long long *groups, unsigned long long *exact);
+
+/* No counterpart in the reference: a self-check of the tensor-core operand
+ * layout.  d (128 x 256 floats, row-major) = a (128 x 64 FP16, row-major) times
+ * the transpose of b (256 x 64 FP16, row-major), computed through shared
+ * memory, tcgen05.mma and tensor memory on the current device.  Device
+ * pointers; synchronises `stream`. */
+bm4dof_status bm4dof_tc_selftest(const void *a, const void *b, float *d, void *stream);
+
 /* Training pairs for the gain network.  Searches the groups of the learned
  * form on `noisy` (grey, params2's geometry, mask switch-offs applied) and
  * writes, for every grid group g of all tiles in processing order:
