@@ -44,7 +44,8 @@ EXPORTS = [
     "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run", "bm4dof_process",
     "bm4dof_set_memory_limit", "bm4dof_plan",
     "bm4dof_get_groups", "bm4dof_last_timings", "bm4dof_search_groups_noalloc",
-    "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_gain_samples",
+    "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_mixed_stats", "bm4dof_tc_selftest",
+    "bm4dof_gain_samples",
     "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_params", "bm4dof_trainer_state",
     "bm4dof_trainer_grad",
     "bm4dof_trainer_step", "bm4dof_trainer_predict", "bm4dof_run_batched", "bm4dof_autotune",
@@ -189,6 +190,10 @@ def load(path: str = LIB_PATH):
     L.bm4dof_set_gain_network.restype = C.c_int
     L.bm4dof_learned_stats.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]
     L.bm4dof_learned_stats.restype = C.c_int
+    L.bm4dof_mixed_stats.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]
+    L.bm4dof_mixed_stats.restype = C.c_int
+    L.bm4dof_tc_selftest.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.bm4dof_tc_selftest.restype = C.c_int
     L.bm4dof_gain_samples.argtypes = [C.c_void_p] * 5 + [C.c_uint] * 3 + [
         C.POINTER(Params), C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
         C.POINTER(C.c_size_t)]
@@ -423,6 +428,13 @@ class Context:
         _check(load().bm4dof_learned_stats(self._h, C.byref(g), C.byref(f)))
         return g.value, f.value
 
+    def mixed_stats(self):
+        """(groups searched through the tensor-core pre-screen, groups of those
+        left to the exact search) of the last mixed-precision run."""
+        g, e = C.c_ulonglong(), C.c_ulonglong()
+        _check(load().bm4dof_mixed_stats(self._h, C.byref(g), C.byref(e)))
+        return g.value, e.value
+
     def gain_samples(self, noisy, basic, fflow, bflow, p2, nparts=2):
         """Training pairs of the gain network for one grey video (CUDA
         tensors (F, 1, H, W)): returns (features [n, 65], targets [n, 64]) as
@@ -528,6 +540,19 @@ def runNlBayes(noisy, fflow, bflow, p1, p2, basic=None, nparts=2, **kw):
     if _default is None:
         _default = Context(0)
     return _default.runNlBayes(noisy, fflow, bflow, p1, p2, basic=basic, nparts=nparts, **kw)
+
+
+def tc_selftest(a, b):
+    """D = a @ b.T through tcgen05.mma (bm4dof_tc_selftest): a [128, 64] and
+    b [256, 64] float16 CUDA tensors; returns D [128, 256] float32."""
+    import torch
+    a = a.contiguous()
+    b = b.contiguous()
+    d = torch.empty((128, 256), dtype=torch.float32, device=a.device)
+    stream = torch.cuda.current_stream(a.device).cuda_stream
+    _check(load().bm4dof_tc_selftest(C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+                                     C.c_void_p(d.data_ptr()), C.c_void_p(stream)))
+    return d
 
 
 def plan(W, H, F, params, nparts=2, crop=None, process=False):

@@ -176,7 +176,9 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 	float *dv = reinterpret_cast<float *>(sm + kOffDv);
 	short4 *wt = reinterpret_cast<short4 *>(sm + kOffWt);
 
-	__shared__ __align__(8) uint64_t mma_done[2], epi_done[2];
+	// per operand buffer: MMA finished, norms written (staging warps), read out
+	// (selection warps)
+	__shared__ __align__(8) uint64_t mma_done[2], qn_full[2], epi_done[2];
 	__shared__ uint32_t tmem_base;
 	__shared__ Union uni[kMaxWt];
 	__shared__ int s_nch[kMaxWt];
@@ -196,6 +198,8 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 	if (tid == 0) {
 		umma::mbar_init(&mma_done[0], 1);
 		umma::mbar_init(&mma_done[1], 1);
+		umma::mbar_init(&qn_full[0], 128);
+		umma::mbar_init(&qn_full[1], 128);
 		umma::mbar_init(&epi_done[0], 4);
 		umma::mbar_init(&epi_done[1], 4);
 		umma::mbar_init_fence();
@@ -347,7 +351,9 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 					for (int ch = 0; ch < s_nch[ii]; ch++, jchunk++) {
 						const int b = jchunk & 1;
 						const uint32_t par = (jchunk >> 1) & 1;
-						if (!umma::mbar_wait(&mma_done[b], par, kWaitLimit)) atomicOr(&s_fail, 1);
+						if (!umma::mbar_wait(&qn_full[b], par, kWaitLimit) ||
+						    !umma::mbar_wait(&mma_done[b], par, kWaitLimit))
+							atomicOr(&s_fail, 1);
 						umma::fence_after_sync();
 						const float *qn = qnc + b * kN;
 						const int n0 = ch * kN;
@@ -482,6 +488,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 							}
 						}
 						umma::fence_proxy_async();
+						umma::mbar_arrive(&qn_full[b]);
 						asm volatile("bar.sync 1, 128;" ::: "memory");
 						if (pt == 0) {
 							umma::fence_after_sync();
@@ -519,8 +526,14 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 		if (s_fail) break;
 	}
 	// a wait that gave up leaves the rest of the work to the exact search:
-	// every reference not written keeps the lower bound the caller set (-1)
+	// every reference not written keeps the bound the caller set (NaN: not
+	// certified); the MMAs still in flight are waited for (bounded) before
+	// the tensor memory is released
 	if (tid == 0 && s_fail) atomicOr(a.status, 1);
+	if (tid == 128 && s_fail) {
+		for (uint32_t j = jchunk >= 2 ? jchunk - 2 : 0; j < jchunk; j++)
+			umma::mbar_wait(&mma_done[j & 1], (j >> 1) & 1, kWaitLimit);
+	}
 	umma::fence_before_sync();
 	__syncthreads();
 	if (warp == 0) {
