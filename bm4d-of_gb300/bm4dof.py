@@ -26,6 +26,7 @@ KEEP_GROUPS = 0x2
 MIXED_PRECISION = 0x4
 LEARNED = 0x8
 VBM3D_SEARCH = 0x10   # the predictive search of the reference's VBM3D_SEARCH build
+MIXED_CERTIFIED = 0x20   # mixed precision with the exact path's neighbour lists
 GAIN_PARAMS = 99136   # floats in a gain-network parameter blob
 
 DCT, BIOR1_5 = 0, 1
@@ -190,7 +191,7 @@ def load(path: str = LIB_PATH):
     L.bm4dof_set_gain_network.restype = C.c_int
     L.bm4dof_learned_stats.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]
     L.bm4dof_learned_stats.restype = C.c_int
-    L.bm4dof_mixed_stats.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]
+    L.bm4dof_mixed_stats.argtypes = [C.c_void_p] + [C.POINTER(C.c_ulonglong)] * 3
     L.bm4dof_mixed_stats.restype = C.c_int
     L.bm4dof_tc_selftest.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.bm4dof_tc_selftest.restype = C.c_int
@@ -217,6 +218,14 @@ def load(path: str = LIB_PATH):
     L.bm4dof_trainer_predict.restype = C.c_int
     _lib = L
     return L
+
+
+def _mixed_flags(mixed):
+    """mixed=True: the mixed-precision form; mixed="certified": the same with
+    the exact path's neighbour lists (BM4DOF_MIXED_CERTIFIED)."""
+    if mixed == "certified":
+        return MIXED_PRECISION | MIXED_CERTIFIED
+    return MIXED_PRECISION if mixed else 0
 
 
 def _check(code):
@@ -333,7 +342,7 @@ class Context:
         CUDA tensors (pass preallocated ones to avoid allocation).
         learned=True runs the learned form (no step-1 pass; the gain network
         installed by set_gain_network, or none)."""
-        flags = (KEEP_GROUPS if keep_groups else 0) | (MIXED_PRECISION if mixed else 0)
+        flags = (KEEP_GROUPS if keep_groups else 0) | _mixed_flags(mixed)
         flags |= (LEARNED if learned else 0) | (VBM3D_SEARCH if vbm3d else 0)
         if _is_cuda_tensor(noisy):
             import torch
@@ -394,7 +403,7 @@ class Context:
         """Denoise many sequences with one CUDA graph (bm4dof_run_batched).
         Returns the per-sequence ratios."""
         arr = self._sequences(items)
-        flags = (MIXED_PRECISION if mixed else 0) | (LEARNED if learned else 0) | (VBM3D_SEARCH if vbm3d else 0)
+        flags = _mixed_flags(mixed) | (LEARNED if learned else 0) | (VBM3D_SEARCH if vbm3d else 0)
         t = None
         if tuning is not None:
             t = Tuning(**tuning) if isinstance(tuning, dict) else tuning
@@ -404,7 +413,7 @@ class Context:
     def autotune(self, items, sample=16, mixed=False, learned=False, vbm3d=False):
         """(best tuning dict, table of (branches, slot_mb, search_ctas, ms))."""
         arr = self._sequences(items)
-        flags = (MIXED_PRECISION if mixed else 0) | (LEARNED if learned else 0) | (VBM3D_SEARCH if vbm3d else 0)
+        flags = _mixed_flags(mixed) | (LEARNED if learned else 0) | (VBM3D_SEARCH if vbm3d else 0)
         best = Tuning()
         table = (C.c_float * (4 * 32))()
         rows = C.c_uint()
@@ -430,10 +439,11 @@ class Context:
 
     def mixed_stats(self):
         """(groups searched through the tensor-core pre-screen, groups of those
-        left to the exact search) of the last mixed-precision run."""
-        g, e = C.c_ulonglong(), C.c_ulonglong()
-        _check(load().bm4dof_mixed_stats(self._h, C.byref(g), C.byref(e)))
-        return g.value, e.value
+        given the exact search, groups kept with an uncertified re-rank) of the
+        last mixed-precision run."""
+        g, e, u = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
+        _check(load().bm4dof_mixed_stats(self._h, C.byref(g), C.byref(e), C.byref(u)))
+        return g.value, e.value, u.value
 
     def gain_samples(self, noisy, basic, fflow, bflow, p2, nparts=2):
         """Training pairs of the gain network for one grey video (CUDA
@@ -470,7 +480,7 @@ class Context:
         """VideoNLB::processNlBayes: the step params.isFirstStep names, over one
         video (numpy (F, C, H, W)) cut from a source as crop (make_crop) says.
         Step 2 reads basic.  Returns (basic, final, groups)."""
-        flags = (KEEP_GROUPS if keep_groups else 0) | (MIXED_PRECISION if mixed else 0)
+        flags = (KEEP_GROUPS if keep_groups else 0) | _mixed_flags(mixed)
         flags |= VBM3D_SEARCH if vbm3d else 0
         noisy = np.ascontiguousarray(noisy, np.float32)
         F, Cc, H, W = noisy.shape

@@ -60,7 +60,7 @@ struct bm4dof_ctx {
 	unsigned long long l_groups = 0, l_fallbacks = 0;
 	// mixed form: groups searched through the tensor-core pre-screen, and the
 	// ones it left to the exact search, over both steps of the last run
-	unsigned long long m_groups = 0, m_exact = 0;
+	unsigned long long m_groups = 0, m_exact = 0, m_uncertified = 0;
 	size_t slot_budget = 0;   // bytes of per-chunk aggregation terms
 	bool fixed_budget = false;   // batched children: slot_budget set by the tuning
 	bool no_marks = false;       // inside a graph capture: no timing events
@@ -322,6 +322,7 @@ struct SampleOut {
 
 struct RunMode {
 	bool mixed = false;     // FP16 pre-screen search (+ BF16 transforms where built)
+	bool certified = false; // mixed: exact search for every group the re-rank cannot certify
 	bool learned = false;   // learned form: groups searched on noisy, gain-network filter
 	bool vbm3d = false;     // predictive search of the reference's VBM3D_SEARCH build
 	float beta1 = 3.f;      // learned form: hard threshold of the non-mean rows
@@ -361,7 +362,7 @@ struct StepState {
 	float *d_lb = nullptr;                          // tc_search: bound on the dropped candidates
 	float *d_wgroup = nullptr;
 	unsigned *d_small = nullptr;          // [0] edges, [3] fallbacks, [4] exact-search list, [5] tc status,
-	                                      // [64..] per-tile counts
+	                                      // [6] uncertified re-ranks, [64..] per-tile counts
 	long long *d_blocks = nullptr;
 	unsigned long long *d_edges = nullptr;
 	float *d_acc = nullptr, *d_wacc = nullptr, *d_vals = nullptr;
@@ -635,7 +636,7 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 			CK(cudaMemsetAsync(S.d_lb, 0xff, sizeof(float) * G, st));   // NaN: not certified
 			CK(launch_search_tc(src, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, S.d_blocks, (long long)S.nblocks, G,
 			                    S.d_cand, S.d_lb, reinterpret_cast<int *>(S.d_small + 5), S.d_nsimp, S.d_idx, S.d_fb,
-			                    S.d_small + 4, ctx->nsm, st));
+			                    S.d_small + 4, S.d_small + 6, mode.certified ? 1 : 0, ctx->nsm, st));
 			CK(launch_search(src, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, 0, G, S.d_nsimp, S.d_idx, nullptr,
 			                 ctx->nsm, st, S.d_fb, S.d_small + 4));
 			ctx->launches += 4;
@@ -783,6 +784,7 @@ float step_ratio(bm4dof_ctx *ctx, int slot)
 	if (S.tc_search) {
 		ctx->m_groups += (unsigned long long)S.G;
 		ctx->m_exact += S.h_small[4];
+		ctx->m_uncertified += S.h_small[6];
 	}
 	return r;
 }
@@ -967,11 +969,11 @@ bm4dof_status validate_run(RunArgs &r, const char *who)
 	}
 	if (r.step != 1 && !r.final_) { set_error(std::string(who) + ": final output is NULL"); return BM4DOF_ERR_ARGUMENT; }
 	if (r.flags & ~(BM4DOF_DEVICE_POINTERS | BM4DOF_KEEP_GROUPS | BM4DOF_MIXED_PRECISION | BM4DOF_LEARNED |
-	                BM4DOF_VBM3D_SEARCH)) {
+	                BM4DOF_VBM3D_SEARCH | BM4DOF_MIXED_CERTIFIED)) {
 		set_error(std::string(who) + ": unsupported flags");
 		return BM4DOF_ERR_UNSUPPORTED;
 	}
-	if ((r.flags & BM4DOF_VBM3D_SEARCH) && (r.flags & (BM4DOF_MIXED_PRECISION | BM4DOF_LEARNED))) {
+	if ((r.flags & BM4DOF_VBM3D_SEARCH) && (r.flags & (BM4DOF_MIXED_PRECISION | BM4DOF_MIXED_CERTIFIED | BM4DOF_LEARNED))) {
 		set_error(std::string(who) + ": the predictive search runs on the plain FP32 path only");
 		return BM4DOF_ERR_UNSUPPORTED;
 	}
@@ -989,7 +991,8 @@ bm4dof_status validate_run(RunArgs &r, const char *who)
 	}
 	r.keep = (r.flags & BM4DOF_KEEP_GROUPS) != 0;
 	r.mode = RunMode();
-	r.mode.mixed = (r.flags & BM4DOF_MIXED_PRECISION) != 0;
+	r.mode.mixed = (r.flags & (BM4DOF_MIXED_PRECISION | BM4DOF_MIXED_CERTIFIED)) != 0;
+	r.mode.certified = (r.flags & BM4DOF_MIXED_CERTIFIED) != 0;
 	r.mode.vbm3d = (r.flags & BM4DOF_VBM3D_SEARCH) != 0;
 	r.mode.beta1 = r.p1.beta;
 	const bool color = r.C > 1;
@@ -1093,7 +1096,7 @@ bm4dof_status launch_run(bm4dof_ctx *ctx, const RunArgs &r)
 bm4dof_status finish_run(bm4dof_ctx *ctx, const RunArgs &r, float ratios[2])
 {
 	float gr[2] = {0.f, 0.f};
-	ctx->m_groups = ctx->m_exact = 0;
+	ctx->m_groups = ctx->m_exact = ctx->m_uncertified = 0;
 	if (r.run1) gr[0] = step_ratio(ctx, 0);
 	if (r.run2) gr[1] = step_ratio(ctx, 1);
 	if (r.keep) {
@@ -1457,7 +1460,8 @@ bm4dof_status bm4dof_run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigne
 		set_error("bm4dof_run_batched: null context or no sequences");
 		return BM4DOF_ERR_ARGUMENT;
 	}
-	if (flags & ~(BM4DOF_MIXED_PRECISION | BM4DOF_LEARNED | BM4DOF_DEVICE_POINTERS | BM4DOF_VBM3D_SEARCH)) {
+	if (flags & ~(BM4DOF_MIXED_PRECISION | BM4DOF_MIXED_CERTIFIED | BM4DOF_LEARNED | BM4DOF_DEVICE_POINTERS |
+	              BM4DOF_VBM3D_SEARCH)) {
 		set_error("bm4dof_run_batched: unsupported flags");
 		return BM4DOF_ERR_UNSUPPORTED;
 	}
@@ -1594,12 +1598,14 @@ bm4dof_status bm4dof_learned_stats(bm4dof_ctx *ctx, unsigned long long *groups, 
 	return BM4DOF_OK;
 }
 
-bm4dof_status bm4dof_mixed_stats(bm4dof_ctx *ctx, unsigned long long *groups, unsigned long long *exact)
+bm4dof_status bm4dof_mixed_stats(bm4dof_ctx *ctx, unsigned long long *groups, unsigned long long *exact,
+                                 unsigned long long *uncertified)
 {
 	CtxLock lock_(ctx);
 	if (!ctx) return BM4DOF_ERR_ARGUMENT;
 	if (groups) *groups = ctx->m_groups;
 	if (exact) *exact = ctx->m_exact;
+	if (uncertified) *uncertified = ctx->m_uncertified;
 	return BM4DOF_OK;
 }
 

@@ -30,10 +30,14 @@
 //    32 candidates in the reference's summation order, sorted.  When the k
 //    smallest are pairwise distinct, below the next one and below L, no
 //    dropped candidate can be among them or tie with them, so they are
-//    exactly what std::partial_sort returns; the tau rule follows.  Every
-//    other reference (a tie, L too low, a NaN, or a block whose windows do not
-//    fit the staging buffer) goes on a list for the exact search
-//    (search.cu), so the neighbour lists are always the exact path's.
+//    exactly what std::partial_sort returns; the tau rule follows.  A
+//    reference whose pre-screen did not finish (a NaN, a value beyond FP16,
+//    or a block whose windows do not fit the staging buffer) goes on a list
+//    for the exact search (search.cu).  One that is merely not certified (a
+//    tie, or L too low: near-equal candidates, as in flat regions of the
+//    basic estimate) keeps the order of its re-ranked 32 by default, or goes
+//    on that list too when every neighbour list must be the exact path's
+//    (BM4DOF_MIXED_CERTIFIED).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -58,7 +62,6 @@ constexpr int kMaxWt = 16;            // candidate frames per reference on this 
 constexpr int kWinHalves = 23552;     // staged window capacity (FP16 values)
 constexpr int kTmemCols = 512;        // two accumulators of kN columns
 constexpr uint32_t kWaitLimit = 1u << 22;   // mbarrier polls before giving up
-constexpr float kShift = 128.f;
 
 // byte offsets of the dynamic shared memory
 constexpr int kOffA = 0;                                  // 128 x 64 FP16, core-matrix layout
@@ -147,14 +150,20 @@ __device__ __forceinline__ float build_rows(RowFn rows, int x, int part, unsigne
 }
 
 // Lower bound on the reference FP32 distance of every candidate whose
-// approximate distance is at least a32 (see the file comment).
-__device__ __forceinline__ float drop_bound(float a32, float pn, float qmax)
+// approximate distance is at least a32 (see the file comment): dp is the
+// exact norm of the reference patch's FP16 rounding error, emax the largest
+// rounding error of any staged window value (a candidate's error norm is at
+// most 8 emax), pn and qmax the patch norms of the split.
+__device__ __forceinline__ float drop_bound(float a32, float pn, float qmax, float dp, float emax)
 {
-	if (a32 != a32 || pn != pn || qmax != qmax) return -1.f;
+	if (a32 != a32 || pn != pn || qmax != qmax || dp != dp || emax != emax) return -1.f;
 	if (a32 == __int_as_float(0x7f800000)) return a32;     // fewer than 32 candidates: none dropped
 	const float sp = sqrtf(fmaxf(pn, 0.f)), sq = sqrtf(fmaxf(qmax, 0.f));
-	const float e = 3.0e-5f * (sp + sq) * (sp + sq) + 1e-2f;
-	const float delta = 5.0e-4f * (sp + sq) + 5e-4f;
+	// FP32 rounding of the norms (64-term chains), of the tensor-core dot
+	// product (64 additions) and of the sums that form the keys
+	const float e = 1.0e-5f * (sp + sq) * (sp + sq) + 1e-2f;
+	// FP16 rounding of both patches
+	const float delta = 1.01f * (dp + 8.f * emax) + 1e-4f;
 	const float r = a32 - e;
 	if (!(r > 0.f)) return 0.f;
 	const float d = sqrtf(r) * 0.99999f - delta;
@@ -182,10 +191,10 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 	__shared__ uint32_t tmem_base;
 	__shared__ Union uni[kMaxWt];
 	__shared__ int s_nch[kMaxWt];
-	__shared__ float s_pn[kRefs];
+	__shared__ float s_pn[kRefs], s_dp[kRefs];
 	__shared__ long long s_g[kRefs];
 	__shared__ int s_x[kRefs], s_y[kRefs];
-	__shared__ int s_overflow, s_qmax, s_fail, s_bad;
+	__shared__ int s_overflow, s_qmax, s_fail, s_bad, s_emax, s_csum, s_ccnt;
 
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const bool selector = warp < 4;
@@ -239,8 +248,32 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 			s_overflow = 0;
 			s_qmax = 0;
 			s_bad = 0;
+			s_emax = 0;
+			s_csum = 0;
+			s_ccnt = 0;
 		}
 		__syncthreads();
+		if (tid < kRefs) {
+			// the block's centre: the rounded mean of its reference positions'
+			// values (integer sums: the same centre on every run)
+			int v = 0, n = 0;
+			if (s_g[tid] >= 0) {
+				const float f = __ldg(src.p + src.at(T.ox + s_x[tid], T.oy + s_y[tid], tr, 0));
+				v = __float2int_rn(fminf(fmaxf(f, -30000.f), 30000.f));
+				n = 1;
+			}
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) {
+				v += __shfl_xor_sync(0xffffffffu, v, o);
+				n += __shfl_xor_sync(0xffffffffu, n, o);
+			}
+			if (lane == 0) {
+				atomicAdd(&s_csum, v);
+				atomicAdd(&s_ccnt, n);
+			}
+		}
+		__syncthreads();
+		const float centre = s_ccnt > 0 ? (float)__float2int_rn((float)s_csum / (float)s_ccnt) : 128.f;
 		if (selector) {
 			// windows of every candidate frame (nldct.cpp:1248-1258) and their union
 			const long long g = s_g[tid];
@@ -284,7 +317,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 			const int pt = tid - 128;
 			for (int it = pt; it < kRefs * 4; it += 128) {
 				const int r = it >> 2, part = it & 3;
-				float s = 0.f;
+				float s = 0.f, er = 0.f;
 				if (s_g[r] >= 0) {
 					const int x = T.ox + s_x[r], y = T.oy + s_y[r];
 					float v[16];
@@ -293,7 +326,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 						int ht, hy, hx;
 						if (PX == 4) { ht = part; hy = e >> 2; hx = e & 3; }
 						else { ht = 0; hy = 2 * part + (e >> 3); hx = e & 7; }
-						v[e] = __ldg(src.p + src.at(x + hx, y + hy, tr + ht, 0)) - kShift;
+						v[e] = __ldg(src.p + src.at(x + hx, y + hy, tr + ht, 0)) - centre;
 					}
 					bool fin = true;
 #pragma unroll
@@ -305,6 +338,9 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 						const __half2 p2 = __floats2half2_rn(v[2 * e], v[2 * e + 1]);
 						h[e] = *reinterpret_cast<const uint32_t *>(&p2);
 						s = sq_half2(h[e], s);
+						const float2 f = __half22float2(p2);
+						const float e0 = f.x - v[2 * e], e1 = f.y - v[2 * e + 1];
+						er = fmaf(e1, e1, fmaf(e0, e0, er));
 					}
 					*reinterpret_cast<uint4 *>(sA + cm_off(r, 2 * part)) = make_uint4(h[0], h[1], h[2], h[3]);
 					*reinterpret_cast<uint4 *>(sA + cm_off(r, 2 * part + 1)) = make_uint4(h[4], h[5], h[6], h[7]);
@@ -315,7 +351,12 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 				// the four parts of a reference are in consecutive threads
 				s += __shfl_xor_sync(0xffffffffu, s, 1);
 				s += __shfl_xor_sync(0xffffffffu, s, 2);
-				if (part == 0) s_pn[r] = s;
+				er += __shfl_xor_sync(0xffffffffu, er, 1);
+				er += __shfl_xor_sync(0xffffffffu, er, 2);
+				if (part == 0) {
+					s_pn[r] = s;
+					s_dp[r] = sqrtf(er);
+				}
 			}
 			umma::fence_proxy_async();
 		}
@@ -450,12 +491,19 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 						const int ht = row / wh, y = row - ht * wh;
 						const float *gp = src.p + src.at(T.ox + u.x0, T.oy + u.y0 + y, qt + ht, 0);
 						__half2 *dp = reinterpret_cast<__half2 *>(win + (ht * wh + y) * pitch);
+						float em = 0.f;
 						for (int x2 = lane; 2 * x2 < ww; x2 += 32) {
-							const float v0 = __ldg(gp + 2 * x2) - kShift;
-							const float v1 = 2 * x2 + 1 < ww ? __ldg(gp + 2 * x2 + 1) - kShift : 0.f;
+							const float v0 = __ldg(gp + 2 * x2) - centre;
+							const float v1 = 2 * x2 + 1 < ww ? __ldg(gp + 2 * x2 + 1) - centre : 0.f;
 							if (!(fabsf(v0) < 60000.f && fabsf(v1) < 60000.f)) s_bad = 1;
-							dp[x2] = __floats2half2_rn(v0, v1);
+							const __half2 h2 = __floats2half2_rn(v0, v1);
+							const float2 f = __half22float2(h2);
+							em = fmaxf(em, fmaxf(fabsf(f.x - v0), fabsf(f.y - v1)));
+							dp[x2] = h2;
 						}
+#pragma unroll
+						for (int o = 16; o > 0; o >>= 1) em = fmaxf(em, __shfl_xor_sync(0xffffffffu, em, o));
+						if (lane == 0) atomicMax(&s_emax, __float_as_int(em));
 					}
 					asm volatile("bar.sync 1, 128;" ::: "memory");
 					const int nu = UW * UH;
@@ -512,7 +560,9 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 			if (g >= 0) {
 				const float root = hd[tid];
 				const bool skip = overflow || s_bad;
-				const float lbv = skip ? -1.f : drop_bound(root + s_pn[tid], s_pn[tid], __int_as_float(s_qmax));
+				const float lbv = skip ? -1.f
+				                       : drop_bound(root + s_pn[tid], s_pn[tid], __int_as_float(s_qmax), s_dp[tid],
+				                                    __int_as_float(s_emax));
 				a.lb[g] = lbv;
 				uint4 *out = reinterpret_cast<uint4 *>(a.cand + g * kTop);
 				for (int s = 0; s < kTop; s += 4)
@@ -555,6 +605,8 @@ struct RerankArgs {
 	uint32_t *idx;
 	uint32_t *fallback;       // groups left to the exact search
 	unsigned *nfallback;
+	unsigned *nuncertified;   // groups kept with their uncertified re-rank
+	int certified;            // 1: every group not certified goes to the exact search
 };
 
 __device__ __forceinline__ bool key_less(float d0, int c0, float d1, int c1)
@@ -646,9 +698,11 @@ __global__ void __launch_bounds__(256) rerank_kernel(Image src, StepParams sp, R
 		const bool distinct = !inside || lane + 1 >= 32 || dnext > d;
 		const float dk = __shfl_sync(0xffffffffu, d, max(Kk - 1, 0));
 		const int nlisted = __popc(__ballot_sync(0xffffffffu, has));
-		const bool ok = !nan && lbv >= 0.f && __all_sync(0xffffffffu, distinct) &&
-		                (ncand <= kTop ? nlisted == ncand : dk < lbv) && Kk > 0;
-		if (ok) {
+		// usable: a finished pre-screen with no NaN; certified: see above
+		const bool usable = !nan && lbv >= 0.f && Kk > 0 && nlisted >= Kk;
+		const bool ok = usable && __all_sync(0xffffffffu, distinct) && (ncand <= kTop ? nlisted == ncand : dk < lbv);
+		if (ok || (usable && !a.certified)) {
+			if (!ok && lane == 0) atomicAdd(a.nuncertified, 1u);
 			float dn[5];
 			dn[0] = __shfl_sync(0xffffffffu, d, 1);
 			dn[1] = __shfl_sync(0xffffffffu, d, 2);
@@ -767,7 +821,8 @@ size_t tc_smem_bytes() { return (size_t)kSmem; }
 cudaError_t launch_search_tc(const Image &src, const Tile *tiles, int ntiles, const int *grid, const uint32_t *traj,
                              const StepParams &sp, const long long *blocks, long long nblocks, long long G,
                              uint32_t *cand, float *lb, int *status, uint8_t *nsimp, uint32_t *idx,
-                             uint32_t *fallback, unsigned *nfallback, int nsm, cudaStream_t st)
+                             uint32_t *fallback, unsigned *nfallback, unsigned *nuncertified, int certified, int nsm,
+                             cudaStream_t st)
 {
 	if (G <= 0) return cudaSuccess;
 	TcArgs ta;
@@ -794,6 +849,8 @@ cudaError_t launch_search_tc(const Image &src, const Tile *tiles, int ntiles, co
 	ra.idx = idx;
 	ra.fallback = fallback;
 	ra.nfallback = nfallback;
+	ra.nuncertified = nuncertified;
+	ra.certified = certified;
 	return sp.px == 4 ? launch_tc_t<4, 4>(src, sp, ta, ra, nsm, st) : launch_tc_t<8, 1>(src, sp, ta, ra, nsm, st);
 }
 

@@ -142,6 +142,11 @@ bm4dof_status bm4dof_set_memory_limit(bm4dof_ctx *ctx, size_t bytes);
  * of the pool kept.  Exact: the same neighbours as that build.  Plain FP32
  * path only (not with BM4DOF_MIXED_PRECISION or BM4DOF_LEARNED). */
 #define BM4DOF_VBM3D_SEARCH     0x10u
+/* BM4DOF_MIXED_PRECISION whose patch search returns the exact path's
+ * neighbour lists: every group whose tensor-core pre-screen cannot be
+ * certified (near-equal candidates) gets the exact search.  Implies
+ * BM4DOF_MIXED_PRECISION. */
+#define BM4DOF_MIXED_CERTIFIED  0x20u
 
 /* VideoNLB::runNlBayes, src/core/nldct.cpp:267-478.
  *
@@ -348,11 +353,15 @@ bm4dof_status bm4dof_set_gain_network(bm4dof_ctx *ctx, const float *params, size
 bm4dof_status bm4dof_learned_stats(bm4dof_ctx *ctx, unsigned long long *groups,
                                    unsigned long long *fallbacks);
 
-/* No counterpart in the reference.  Groups whose patch search went through
- * the tensor-core pre-screen in the last BM4DOF_MIXED_PRECISION run (both
- * steps), and how many of them the certified re-rank left to the exact
- * search.  Either way the neighbour lists are the exact search's. */
-bm4dof_status bm4dof_mixed_stats(bm4dof_ctx *ctx, unsigned long long *groups, unsigned long long *exact);
+/* No counterpart in the reference.  Over both steps of the last
+ * BM4DOF_MIXED_PRECISION run: the groups whose patch search went through the
+ * tensor-core pre-screen; of those, the ones that got the exact search
+ * instead (pre-screen unusable, or not certified under
+ * BM4DOF_MIXED_CERTIFIED); and the ones that kept an uncertified re-rank of
+ * their 32 best approximations (only without BM4DOF_MIXED_CERTIFIED).  Every
+ * other group's neighbour list is certified to be the exact path's. */
+bm4dof_status bm4dof_mixed_stats(bm4dof_ctx *ctx, unsigned long long *groups, unsigned long long *exact,
+                                 unsigned long long *uncertified);
 
 /* No counterpart in the reference: a self-check of the tensor-core operand
  * layout.  d (128 x 256 floats, row-major) = a (128 x 64 FP16, row-major) times

@@ -1,14 +1,19 @@
 """Mixed-precision form: the patch search on the Blackwell tensor cores
 (tcgen05.mma, FP16 operands, FP32 accumulation in tensor memory) as a
 pre-screen, then the exact FP32 distances of the 32 best candidates,
-certified against a bound on every dropped one; groups it cannot certify get
-the exact search.  The neighbour lists are therefore the exact search's, and
-with the FP32 group filter the output is the plain path's, bit for bit."""
+certified against a bound on every dropped one.
+
+* BM4DOF_MIXED_CERTIFIED: groups it cannot certify get the exact search, so
+  the neighbour lists are the exact search's and (with the FP32 group filter)
+  the output is the plain path's, bit for bit.
+* BM4DOF_MIXED_PRECISION: an uncertified group keeps the order of its
+  re-ranked 32; the bars are neighbour sets that agree with the exact path
+  and a PSNR change far inside 0.05 dB."""
 import numpy as np
 import pytest
 
 from cases import CFG_IMAGE, CFG_VIDEO
-from helpers import resolve_params, video_case
+from helpers import psnr, resolve_params, video_case
 
 pytestmark = pytest.mark.gpu
 
@@ -48,13 +53,43 @@ def test_mixed_search_is_exact(gpulib, gpuctx, cfg, shape, sigma, nparts):
     p = resolve_params(gpulib, (W, H, F, 1), sigma, **cfg)
     pb, pf, pr = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=nparts, keep_groups=True)
     plain = lists(gpuctx, nparts)
-    mb, mf, mr = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=nparts, keep_groups=True, mixed=True)
-    groups, exact = gpuctx.mixed_stats()
-    assert groups > 0
+    mb, mf, mr = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=nparts, keep_groups=True, mixed="certified")
+    groups, exact, uncertified = gpuctx.mixed_stats()
+    assert groups > 0 and uncertified == 0
     same_lists(plain, lists(gpuctx, nparts))
     assert np.array_equal(pb, mb) and np.array_equal(pf, mf) and pr == mr
-    # most groups are certified by the pre-screen
-    assert exact <= 0.25 * groups, (exact, groups)
+    # the pre-screen certifies most groups (near-equal candidates in the smooth
+    # basic estimate are the ones it leaves to the exact search)
+    assert exact <= 0.6 * groups, (exact, groups)
+
+
+def set_agreement(a, b):
+    same = total = 0
+    for ta, tb in zip(a, b):
+        assert np.array_equal(ta["ref"], tb["ref"])
+        for i in range(len(ta["ref"])):
+            sa = set(ta["index"][i, :ta["nsimp"][i]].tolist())
+            sb = set(tb["index"][i, :tb["nsimp"][i]].tolist())
+            same += sa == sb
+            total += 1
+    return same / max(total, 1)
+
+
+@pytest.mark.parametrize("shape,sigma", [((64, 48, 8), 20.0), ((160, 96, 10), 10.0), ((120, 88, 12), 40.0)],
+                         ids=["s20", "s10", "s40"])
+def test_mixed_search_default_agrees(gpulib, gpuctx, shape, sigma):
+    W, H, F = shape
+    clean, nz, ff, bf = video_case(W, H, F, sigma=sigma, seed=78)
+    p = resolve_params(gpulib, (W, H, F, 1), sigma, **CFG_VIDEO)
+    pb, pf, pr = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=2, keep_groups=True)
+    plain = lists(gpuctx, 2)
+    mb, mf, mr = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=2, keep_groups=True, mixed=True)
+    groups, exact, uncertified = gpuctx.mixed_stats()
+    mixed = lists(gpuctx, 2)
+    # step 1 searches the same noisy video: its sets agree almost everywhere
+    assert set_agreement(plain[0], mixed[0]) >= 0.995
+    assert abs(psnr(pf, clean) - psnr(mf, clean)) <= 0.01
+    assert exact + uncertified <= groups
 
 
 def test_mixed_search_ties_fall_back_to_exact(gpulib, gpuctx):
@@ -69,8 +104,8 @@ def test_mixed_search_ties_fall_back_to_exact(gpulib, gpuctx):
     p = resolve_params(gpulib, (W, H, F, 1), 10.0, **CFG_VIDEO)
     a = gpuctx.runNlBayes(nz, None, None, *p, nparts=2, keep_groups=True)
     plain = lists(gpuctx, 2)
-    b = gpuctx.runNlBayes(nz, None, None, *p, nparts=2, keep_groups=True, mixed=True)
-    groups, exact = gpuctx.mixed_stats()
+    b = gpuctx.runNlBayes(nz, None, None, *p, nparts=2, keep_groups=True, mixed="certified")
+    groups, exact, uncertified = gpuctx.mixed_stats()
     assert exact > 0
     same_lists(plain, lists(gpuctx, 2))
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
