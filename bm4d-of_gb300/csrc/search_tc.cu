@@ -72,7 +72,10 @@ constexpr int kOffHd = kOffQn + 2 * kN * 4;               // heaps: 32 x 128 key
 constexpr int kOffHc = kOffHd + kTop * kRefs * 4;         // heaps: 32 x 128 candidates
 constexpr int kOffDv = kOffHc + kTop * kRefs * 4;         // 4 warps x 32 lanes x 36 keys
 constexpr int kOffWt = kOffDv + 4 * 32 * 36 * 4;          // windows: kMaxWt x 128 x short4
-constexpr int kSmem = kOffWt + kMaxWt * kRefs * 8;
+constexpr int kQ = 8;                                     // pending heap insertions per reference
+constexpr int kOffQk = kOffWt + kMaxWt * kRefs * 8;       // pending keys: kQ x 128
+constexpr int kOffQc = kOffQk + kQ * kRefs * 4;           // pending candidates: kQ x 128
+constexpr int kSmem = kOffQc + kQ * kRefs * 4;
 
 static_assert(kSmem <= 227 * 1024, "shared memory");
 
@@ -171,6 +174,38 @@ __device__ __forceinline__ float drop_bound(float a32, float pn, float qmax, flo
 	return d * d * 0.9999f;
 }
 
+// Inserts a reference's pending candidates into its max-heap of kTop (keys
+// hd, candidates hc, one column per reference); returns the new root.
+__device__ __forceinline__ float flush_queue(float *hd, uint32_t *hc, const float *qk, const uint32_t *qc, int r,
+                                            int &qlen, float thr)
+{
+	for (int i = 0; i < qlen; i++) {
+		const float d = qk[i * kRefs + r];
+		if (!(d < thr)) continue;
+		const uint32_t cid = qc[i * kRefs + r];
+		int pos = 0;
+		for (;;) {
+			const int l = 2 * pos + 1;
+			if (l >= kTop) break;
+			int chd = l;
+			float cd = hd[l * kRefs + r];
+			if (l + 1 < kTop) {
+				const float rd = hd[(l + 1) * kRefs + r];
+				if (rd > cd) { chd = l + 1; cd = rd; }
+			}
+			if (!(cd > d)) break;
+			hd[pos * kRefs + r] = cd;
+			hc[pos * kRefs + r] = hc[chd * kRefs + r];
+			pos = chd;
+		}
+		hd[pos * kRefs + r] = d;
+		hc[pos * kRefs + r] = cid;
+		thr = hd[r];
+	}
+	qlen = 0;
+	return thr;
+}
+
 template <int PX, int PT>
 __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepParams sp, TcArgs a)
 {
@@ -184,6 +219,8 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 	uint32_t *hc = reinterpret_cast<uint32_t *>(sm + kOffHc);
 	float *dv = reinterpret_cast<float *>(sm + kOffDv);
 	short4 *wt = reinterpret_cast<short4 *>(sm + kOffWt);
+	float *qk = reinterpret_cast<float *>(sm + kOffQk);
+	uint32_t *qc = reinterpret_cast<uint32_t *>(sm + kOffQc);
 
 	// per operand buffer: MMA finished, norms written (staging warps), read out
 	// (selection warps)
@@ -381,6 +418,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 				const int r = tid;
 				const bool valid = s_g[r] >= 0;
 				float thr = __int_as_float(0x7f800000);   // heap root, keys |q'|^2 - 2<p',q'>
+				int qlen = 0;                              // pending insertions
 				const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
 				float *mydv = dv + (warp * 32 + lane) * 36;
 				for (int ii = 0; ii < nwt; ii++) {
@@ -440,34 +478,24 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 									*reinterpret_cast<float4 *>(mydv + 4 * c4) =
 										make_float4(key[4 * c4], key[4 * c4 + 1], key[4 * c4 + 2], key[4 * c4 + 3]);
 							}
-							while (hits) {
-								const int c = __ffs(hits) - 1;
-								hits &= hits - 1u;
-								const float d = mydv[c];
-								if (!(d < thr)) continue;
-								int tx = col0 + c, ty = row0;
-								while (tx >= UW) { tx -= UW; ty++; }
-								const uint32_t cid = (uint32_t)(u.x0 + tx) | ((uint32_t)(u.y0 + ty) << 13) |
-								                     ((uint32_t)ii << 26);
-								// replace the root of the max-heap and sift down
-								int pos = 0;
-								for (;;) {
-									const int l = 2 * pos + 1;
-									if (l >= kTop) break;
-									int chd = l;
-									float cd = hd[l * kRefs + r];
-									if (l + 1 < kTop) {
-										const float rd = hd[(l + 1) * kRefs + r];
-										if (rd > cd) { chd = l + 1; cd = rd; }
+							// hits wait in a short queue per reference; when any queue is
+							// full the warp inserts all of them together, so that one
+							// pass of heap updates serves every lane
+							while (__any_sync(0xffffffffu, hits)) {
+								if (hits) {
+									const int c = __ffs(hits) - 1;
+									hits &= hits - 1u;
+									const float d = mydv[c];
+									if (d < thr) {
+										int tx = col0 + c, ty = row0;
+										while (tx >= UW) { tx -= UW; ty++; }
+										qk[qlen * kRefs + r] = d;
+										qc[qlen * kRefs + r] = (uint32_t)(u.x0 + tx) | ((uint32_t)(u.y0 + ty) << 13) |
+										                       ((uint32_t)ii << 26);
+										qlen++;
 									}
-									if (!(cd > d)) break;
-									hd[pos * kRefs + r] = cd;
-									hc[pos * kRefs + r] = hc[chd * kRefs + r];
-									pos = chd;
 								}
-								hd[pos * kRefs + r] = d;
-								hc[pos * kRefs + r] = cid;
-								thr = hd[r];
+								if (__any_sync(0xffffffffu, qlen == kQ)) thr = flush_queue(hd, hc, qk, qc, r, qlen, thr);
 							}
 						}
 						umma::fence_before_sync();
@@ -475,6 +503,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 						if (lane == 0) umma::mbar_arrive(&epi_done[b]);
 					}
 				}
+				thr = flush_queue(hd, hc, qk, qc, r, qlen, thr);
 			} else {
 				// staging warps: window of every candidate frame, then its chunks
 				const int pt = tid - 128, pw = pt >> 5;
@@ -487,19 +516,38 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 					const int wh = UH + PX - 1, ww = UW + PX - 1;
 					// the previous frame's chunks are all built: the window can go
 					asm volatile("bar.sync 1, 128;" ::: "memory");
-					for (int row = pw; row < PT * wh; row += 4) {
-						const int ht = row / wh, y = row - ht * wh;
-						const float *gp = src.p + src.at(T.ox + u.x0, T.oy + u.y0 + y, qt + ht, 0);
-						__half2 *dp = reinterpret_cast<__half2 *>(win + (ht * wh + y) * pitch);
+					// eight rows per warp in flight: loads first, then conversions
+					{
 						float em = 0.f;
+						const int nrow = PT * wh;
 						for (int x2 = lane; 2 * x2 < ww; x2 += 32) {
-							const float v0 = __ldg(gp + 2 * x2) - centre;
-							const float v1 = 2 * x2 + 1 < ww ? __ldg(gp + 2 * x2 + 1) - centre : 0.f;
-							if (!(fabsf(v0) < 60000.f && fabsf(v1) < 60000.f)) s_bad = 1;
-							const __half2 h2 = __floats2half2_rn(v0, v1);
-							const float2 f = __half22float2(h2);
-							em = fmaxf(em, fmaxf(fabsf(f.x - v0), fabsf(f.y - v1)));
-							dp[x2] = h2;
+							const bool two = 2 * x2 + 1 < ww;
+							for (int r0 = pw; r0 < nrow; r0 += 32) {
+								float v0[8], v1[8];
+#pragma unroll
+								for (int k = 0; k < 8; k++) {
+									const int row = r0 + 4 * k;
+									v0[k] = v1[k] = 0.f;
+									if (row < nrow) {
+										const int ht = row / wh, y = row - ht * wh;
+										const float *gp = src.p + src.at(T.ox + u.x0 + 2 * x2, T.oy + u.y0 + y, qt + ht, 0);
+										v0[k] = __ldg(gp);
+										if (two) v1[k] = __ldg(gp + 1);
+									}
+								}
+#pragma unroll
+								for (int k = 0; k < 8; k++) {
+									const int row = r0 + 4 * k;
+									if (row < nrow) {
+										const float a0 = v0[k] - centre, a1 = two ? v1[k] - centre : 0.f;
+										if (!(fabsf(a0) < 60000.f && fabsf(a1) < 60000.f)) s_bad = 1;
+										const __half2 h2 = __floats2half2_rn(a0, a1);
+										const float2 f = __half22float2(h2);
+										em = fmaxf(em, fmaxf(fabsf(f.x - a0), fabsf(f.y - a1)));
+										reinterpret_cast<__half2 *>(win + row * pitch)[x2] = h2;
+									}
+								}
+							}
 						}
 #pragma unroll
 						for (int o = 16; o > 0; o >>= 1) em = fmaxf(em, __shfl_xor_sync(0xffffffffu, em, o));
