@@ -16,7 +16,9 @@
 //    tcgen05.ld, one reference per thread (its TMEM lane):
 //        a(p, q) = |p'|^2 + |q'|^2 - 2 <p', q'>   (the rounded patches),
 //    test the candidate against the thread's own window and keep the 32
-//    smallest a(p, q) in a per-thread max-heap.  Four staging warps build the
+//    smallest a(p, q): candidates under the current 32nd smallest wait in a
+//    list of up to 32 per reference, which the warp merges into the sorted
+//    kept list with bitonic networks when it fills.  Four staging warps build the
 //    next chunk's operands while the selection warps work on the current
 //    one (two operand buffers, two TMEM accumulators of 256 columns,
 //    mbarriers between them).  Per reference it writes the 32 candidates and
@@ -59,7 +61,7 @@ constexpr int kK = 64;                // patch elements (MMA K, four k-steps of 
 constexpr int kThreads = 256;         // warps 0-3 select, warps 4-7 stage and issue
 constexpr int kTop = 32;              // approximate candidates kept per reference
 constexpr int kMaxWt = 16;            // candidate frames per reference on this path
-constexpr int kWinHalves = 23552;     // staged window capacity (FP16 values)
+constexpr int kWinHalves = 16384;     // staged window capacity (FP16 values)
 constexpr int kTmemCols = 512;        // two accumulators of kN columns
 constexpr uint32_t kWaitLimit = 1u << 22;   // mbarrier polls before giving up
 
@@ -68,14 +70,16 @@ constexpr int kOffA = 0;                                  // 128 x 64 FP16, core
 constexpr int kOffB = kOffA + kRefs * kK * 2;             // 2 x 256 x 64 FP16
 constexpr int kOffWin = kOffB + 2 * kN * kK * 2;          // staged window
 constexpr int kOffQn = kOffWin + kWinHalves * 2 + 64;     // 2 x 256 candidate norms
-constexpr int kOffHd = kOffQn + 2 * kN * 4;               // heaps: 32 x 128 keys
-constexpr int kOffHc = kOffHd + kTop * kRefs * 4;         // heaps: 32 x 128 candidates
-constexpr int kOffDv = kOffHc + kTop * kRefs * 4;         // 4 warps x 32 lanes x 36 keys
+// per reference (row of kLs words): the kept 32 (keys and candidates,
+// ascending) and up to 32 newcomers waiting for a merge
+constexpr int kLs = kTop + 1;                             // row stride: rows start in distinct banks
+constexpr int kOffKd = kOffQn + 2 * kN * 4;               // kept keys: 128 x kLs
+constexpr int kOffKc = kOffKd + kRefs * kLs * 4;          // kept candidates
+constexpr int kOffNd = kOffKc + kRefs * kLs * 4;          // newcomer keys
+constexpr int kOffNc = kOffNd + kRefs * kLs * 4;          // newcomer candidates
+constexpr int kOffDv = kOffNc + kRefs * kLs * 4;          // 4 warps x 32 lanes x 36 keys
 constexpr int kOffWt = kOffDv + 4 * 32 * 36 * 4;          // windows: kMaxWt x 128 x short4
-constexpr int kQ = 8;                                     // pending heap insertions per reference
-constexpr int kOffQk = kOffWt + kMaxWt * kRefs * 8;       // pending keys: kQ x 128
-constexpr int kOffQc = kOffQk + kQ * kRefs * 4;           // pending candidates: kQ x 128
-constexpr int kSmem = kOffQc + kQ * kRefs * 4;
+constexpr int kSmem = kOffWt + kMaxWt * kRefs * 8;
 
 static_assert(kSmem <= 227 * 1024, "shared memory");
 
@@ -174,36 +178,58 @@ __device__ __forceinline__ float drop_bound(float a32, float pn, float qmax, flo
 	return d * d * 0.9999f;
 }
 
-// Inserts a reference's pending candidates into its max-heap of kTop (keys
-// hd, candidates hc, one column per reference); returns the new root.
-__device__ __forceinline__ float flush_queue(float *hd, uint32_t *hc, const float *qk, const uint32_t *qc, int r,
-                                            int &qlen, float thr)
+// Warp-cooperative merge of one reference's newcomers (nd/nc, the first
+// `cnt` of its row) into its kept 32 (kd/kc, ascending): the newcomers are
+// sorted by a bitonic network across the lanes, the lane-wise minimum of the
+// kept list and the reversed newcomers is a bitonic sequence holding the 32
+// smallest of both, and a bitonic merge orders it.  Returns the new 32nd
+// smallest key (the threshold for newcomers) to every lane.
+__device__ __forceinline__ float merge_row(float *kd, uint32_t *kc, const float *nd, const uint32_t *nc, int row,
+                                          int cnt)
 {
-	for (int i = 0; i < qlen; i++) {
-		const float d = qk[i * kRefs + r];
-		if (!(d < thr)) continue;
-		const uint32_t cid = qc[i * kRefs + r];
-		int pos = 0;
-		for (;;) {
-			const int l = 2 * pos + 1;
-			if (l >= kTop) break;
-			int chd = l;
-			float cd = hd[l * kRefs + r];
-			if (l + 1 < kTop) {
-				const float rd = hd[(l + 1) * kRefs + r];
-				if (rd > cd) { chd = l + 1; cd = rd; }
-			}
-			if (!(cd > d)) break;
-			hd[pos * kRefs + r] = cd;
-			hc[pos * kRefs + r] = hc[chd * kRefs + r];
-			pos = chd;
+	const int lane = threadIdx.x & 31;
+	float x = lane < cnt ? nd[row * kLs + lane] : __int_as_float(0x7f800000);
+	uint32_t xc = lane < cnt ? nc[row * kLs + lane] : 0xffffffffu;
+#pragma unroll
+	for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+		for (int j = k >> 1; j > 0; j >>= 1) {
+			const float ox = __shfl_xor_sync(0xffffffffu, x, j);
+			const uint32_t oc = __shfl_xor_sync(0xffffffffu, xc, j);
+			const bool up = (lane & k) == 0, low = (lane & j) == 0;
+			if ((low == up) ? (ox < x) : (x < ox)) { x = ox; xc = oc; }
 		}
-		hd[pos * kRefs + r] = d;
-		hc[pos * kRefs + r] = cid;
-		thr = hd[r];
+	float y = kd[row * kLs + lane];
+	uint32_t yc = kc[row * kLs + lane];
+	const float rx = __shfl_sync(0xffffffffu, x, 31 - lane);
+	const uint32_t rc = __shfl_sync(0xffffffffu, xc, 31 - lane);
+	if (rx < y) { y = rx; yc = rc; }
+#pragma unroll
+	for (int j = 16; j > 0; j >>= 1) {
+		const float oy = __shfl_xor_sync(0xffffffffu, y, j);
+		const uint32_t oc = __shfl_xor_sync(0xffffffffu, yc, j);
+		if (((lane & j) == 0) ? (oy < y) : (y < oy)) { y = oy; yc = oc; }
 	}
-	qlen = 0;
-	return thr;
+	kd[row * kLs + lane] = y;
+	kc[row * kLs + lane] = yc;
+	return __shfl_sync(0xffffffffu, y, 31);
+}
+
+// Merges every lane's newcomers whose lane is set in `need` (warp-collective).
+__device__ __forceinline__ void merge_lanes(float *kd, uint32_t *kc, const float *nd, const uint32_t *nc, int warp,
+                                           unsigned need, int &cnt, float &thr)
+{
+	const int lane = threadIdx.x & 31;
+	while (need) {
+		const int L = __ffs(need) - 1;
+		need &= need - 1u;
+		const int cl = __shfl_sync(0xffffffffu, cnt, L);
+		const float t = merge_row(kd, kc, nd, nc, warp * 32 + L, cl);
+		if (lane == L) {
+			thr = t;
+			cnt = 0;
+		}
+	}
 }
 
 template <int PX, int PT>
@@ -215,12 +241,12 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 	unsigned char *sB = sm + kOffB;
 	__half *win = reinterpret_cast<__half *>(sm + kOffWin);
 	float *qnc = reinterpret_cast<float *>(sm + kOffQn);
-	float *hd = reinterpret_cast<float *>(sm + kOffHd);
-	uint32_t *hc = reinterpret_cast<uint32_t *>(sm + kOffHc);
+	float *kd = reinterpret_cast<float *>(sm + kOffKd);
+	uint32_t *kc = reinterpret_cast<uint32_t *>(sm + kOffKc);
+	float *nd = reinterpret_cast<float *>(sm + kOffNd);
+	uint32_t *nc = reinterpret_cast<uint32_t *>(sm + kOffNc);
 	float *dv = reinterpret_cast<float *>(sm + kOffDv);
 	short4 *wt = reinterpret_cast<short4 *>(sm + kOffWt);
-	float *qk = reinterpret_cast<float *>(sm + kOffQk);
-	uint32_t *qc = reinterpret_cast<uint32_t *>(sm + kOffQc);
 
 	// per operand buffer: MMA finished, norms written (staging warps), read out
 	// (selection warps)
@@ -344,10 +370,10 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 					atomicMax(&uni[ii].y1, my1);
 				}
 			}
-			// heaps: 32 empty slots per reference
+			// kept lists: 32 empty slots per reference
 			for (int s = 0; s < kTop; s++) {
-				hd[s * kRefs + tid] = __int_as_float(0x7f800000);
-				hc[s * kRefs + tid] = 0xffffffffu;
+				kd[tid * kLs + s] = __int_as_float(0x7f800000);
+				kc[tid * kLs + s] = 0xffffffffu;
 			}
 		} else {
 			// A operand: the 128 reference patches, centred FP16
@@ -417,8 +443,8 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 			if (selector) {
 				const int r = tid;
 				const bool valid = s_g[r] >= 0;
-				float thr = __int_as_float(0x7f800000);   // heap root, keys |q'|^2 - 2<p',q'>
-				int qlen = 0;                              // pending insertions
+				float thr = __int_as_float(0x7f800000);   // 32nd smallest kept key |q'|^2 - 2<p',q'>
+				int cnt = 0;                               // newcomers waiting for a merge
 				const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
 				float *mydv = dv + (warp * 32 + lane) * 36;
 				for (int ii = 0; ii < nwt; ii++) {
@@ -478,9 +504,8 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 									*reinterpret_cast<float4 *>(mydv + 4 * c4) =
 										make_float4(key[4 * c4], key[4 * c4 + 1], key[4 * c4 + 2], key[4 * c4 + 3]);
 							}
-							// hits wait in a short queue per reference; when any queue is
-							// full the warp inserts all of them together, so that one
-							// pass of heap updates serves every lane
+							// hits join the reference's newcomers; a full list is merged into
+							// the kept 32 by the whole warp
 							while (__any_sync(0xffffffffu, hits)) {
 								if (hits) {
 									const int c = __ffs(hits) - 1;
@@ -489,13 +514,14 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 									if (d < thr) {
 										int tx = col0 + c, ty = row0;
 										while (tx >= UW) { tx -= UW; ty++; }
-										qk[qlen * kRefs + r] = d;
-										qc[qlen * kRefs + r] = (uint32_t)(u.x0 + tx) | ((uint32_t)(u.y0 + ty) << 13) |
-										                       ((uint32_t)ii << 26);
-										qlen++;
+										nd[r * kLs + cnt] = d;
+										nc[r * kLs + cnt] = (uint32_t)(u.x0 + tx) | ((uint32_t)(u.y0 + ty) << 13) |
+										                    ((uint32_t)ii << 26);
+										cnt++;
 									}
 								}
-								if (__any_sync(0xffffffffu, qlen == kQ)) thr = flush_queue(hd, hc, qk, qc, r, qlen, thr);
+								const unsigned full = __ballot_sync(0xffffffffu, cnt == kTop);
+								if (full) merge_lanes(kd, kc, nd, nc, warp, full, cnt, thr);
 							}
 						}
 						umma::fence_before_sync();
@@ -503,7 +529,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 						if (lane == 0) umma::mbar_arrive(&epi_done[b]);
 					}
 				}
-				thr = flush_queue(hd, hc, qk, qc, r, qlen, thr);
+				merge_lanes(kd, kc, nd, nc, warp, __ballot_sync(0xffffffffu, cnt > 0), cnt, thr);
 			} else {
 				// staging warps: window of every candidate frame, then its chunks
 				const int pt = tid - 128, pw = pt >> 5;
@@ -606,7 +632,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 		if (selector) {
 			const long long g = s_g[tid];
 			if (g >= 0) {
-				const float root = hd[tid];
+				const float root = kd[tid * kLs + kTop - 1];
 				const bool skip = overflow || s_bad;
 				const float lbv = skip ? -1.f
 				                       : drop_bound(root + s_pn[tid], s_pn[tid], __int_as_float(s_qmax), s_dp[tid],
@@ -614,10 +640,10 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 				a.lb[g] = lbv;
 				uint4 *out = reinterpret_cast<uint4 *>(a.cand + g * kTop);
 				for (int s = 0; s < kTop; s += 4)
-					out[s / 4] = make_uint4(skip ? 0xffffffffu : hc[s * kRefs + tid],
-					                        skip ? 0xffffffffu : hc[(s + 1) * kRefs + tid],
-					                        skip ? 0xffffffffu : hc[(s + 2) * kRefs + tid],
-					                        skip ? 0xffffffffu : hc[(s + 3) * kRefs + tid]);
+					out[s / 4] = make_uint4(skip ? 0xffffffffu : kc[tid * kLs + s],
+					                        skip ? 0xffffffffu : kc[tid * kLs + s + 1],
+					                        skip ? 0xffffffffu : kc[tid * kLs + s + 2],
+					                        skip ? 0xffffffffu : kc[tid * kLs + s + 3]);
 			}
 		}
 		__syncthreads();
