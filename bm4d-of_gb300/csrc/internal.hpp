@@ -72,7 +72,7 @@ bool tc_supported(const StepParams &sp, const std::vector<Tile> &tiles);
 size_t tc_smem_bytes();
 cudaError_t launch_search_tc(const Image &src, const Tile *tiles, int ntiles, const int *grid, const uint32_t *traj,
                              const StepParams &sp, const long long *blocks, long long nblocks, long long G,
-                             uint32_t *cand, float *lb, int *status, uint8_t *nsimp, uint32_t *idx,
+                             uint32_t *cand, float *lb, float *thr0, int *status, uint8_t *nsimp, uint32_t *idx,
                              uint32_t *fallback, unsigned *nfallback, unsigned *nuncertified, int certified, int nsm,
                              cudaStream_t st);
 cudaError_t tc_selftest(const uint16_t *A, const uint16_t *B, float *D, int *status, cudaStream_t st);

@@ -359,7 +359,7 @@ struct StepState {
 	uint8_t *d_nsimp = nullptr, *d_alive = nullptr, *d_eq = nullptr, *d_killed = nullptr;
 	uint32_t *d_idx = nullptr, *d_traj = nullptr;
 	uint32_t *d_cand = nullptr, *d_fb = nullptr;   // tc_search: candidates, exact-search list
-	float *d_lb = nullptr;                          // tc_search: bound on the dropped candidates
+	float *d_lb = nullptr, *d_thr0 = nullptr;       // tc_search: bound on the dropped candidates, anchors
 	float *d_wgroup = nullptr;
 	unsigned *d_small = nullptr;          // [0] edges, [3] fallbacks, [4] exact-search list, [5] tc status,
 	                                      // [6] uncertified re-ranks, [64..] per-tile counts
@@ -548,6 +548,7 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	if (S.tc_search) {
 		SBUF("tc_cand", (size_t)G * 32, S.d_cand);
 		SBUF("tc_lb", G, S.d_lb);
+		SBUF("tc_thr0", G, S.d_thr0);
 		SBUF("tc_exact", G, S.d_fb);
 	}
 	if (sp.paste) {
@@ -635,11 +636,12 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 			CK(launch_traj(ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp, G, S.d_traj, st));
 			CK(cudaMemsetAsync(S.d_lb, 0xff, sizeof(float) * G, st));   // NaN: not certified
 			CK(launch_search_tc(src, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, S.d_blocks, (long long)S.nblocks, G,
-			                    S.d_cand, S.d_lb, reinterpret_cast<int *>(S.d_small + 5), S.d_nsimp, S.d_idx, S.d_fb,
+			                    S.d_cand, S.d_lb, S.d_thr0, reinterpret_cast<int *>(S.d_small + 5), S.d_nsimp, S.d_idx,
+			                    S.d_fb,
 			                    S.d_small + 4, S.d_small + 6, mode.certified ? 1 : 0, ctx->nsm, st));
 			CK(launch_search(src, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, 0, G, S.d_nsimp, S.d_idx, nullptr,
 			                 ctx->nsm, st, S.d_fb, S.d_small + 4));
-			ctx->launches += 4;
+			ctx->launches += 5;
 		} else if (S.mixed_search) {
 			// FP16 tensor-core pre-screen + exact re-rank of the best 2k
 			CK(launch_traj(ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp, G, S.d_traj, st));

@@ -96,6 +96,7 @@ struct TcArgs {
 	uint32_t *cand;             // [G][32] candidates (qx | qy << 13 | frame << 26)
 	float *lb;                  // [G] lower bound on every dropped candidate's distance
 	int *status;                // [0]: a wait gave up
+	const float *thr0;          // [G] starting threshold (anchor_kernel), distance units
 };
 
 struct Union {
@@ -216,7 +217,7 @@ __device__ __forceinline__ float merge_row(float *kd, uint32_t *kc, const float 
 
 // Merges every lane's newcomers whose lane is set in `need` (warp-collective).
 __device__ __forceinline__ void merge_lanes(float *kd, uint32_t *kc, const float *nd, const uint32_t *nc, int warp,
-                                           unsigned need, int &cnt, float &thr)
+                                           unsigned need, int &cnt, float &thr, float cap)
 {
 	const int lane = threadIdx.x & 31;
 	while (need) {
@@ -225,7 +226,7 @@ __device__ __forceinline__ void merge_lanes(float *kd, uint32_t *kc, const float
 		const int cl = __shfl_sync(0xffffffffu, cnt, L);
 		const float t = merge_row(kd, kc, nd, nc, warp * 32 + L, cl);
 		if (lane == L) {
-			thr = t;
+			thr = fminf(t, cap);
 			cnt = 0;
 		}
 	}
@@ -441,7 +442,10 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 			if (selector) {
 				const int r = tid;
 				const bool valid = s_g[r] >= 0;
-				float thr = __int_as_float(0x7f800000);   // 32nd smallest kept key |q'|^2 - 2<p',q'>
+				// keys |q'|^2 - 2<p',q'> (the approximate distance less |p'|^2); the
+				// anchors' threshold caps the 32nd smallest kept key from the start
+				const float cap = valid ? a.thr0[s_g[r]] - s_pn[r] : __int_as_float(0x7f800000);
+				float thr = cap < __int_as_float(0x7f800000) ? cap : __int_as_float(0x7f800000);
 				int cnt = 0;                               // newcomers waiting for a merge
 				const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
 				for (int ii = 0; ii < nwt; ii++) {
@@ -499,7 +503,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 							// position in the frame's union); a list that would overflow is
 							// first merged into the kept 32 by the whole warp
 							const unsigned over = __ballot_sync(0xffffffffu, cnt + __popc(hits) > kTop);
-							if (over) merge_lanes(kd, kc, nd, nc, warp, over, cnt, thr);
+							if (over) merge_lanes(kd, kc, nd, nc, warp, over, cnt, thr, cap);
 							if (hits) {
 								const uint32_t cbase = ((uint32_t)ii << 16) | (uint32_t)g0c;
 								float *ndr = nd + r * kLs;
@@ -518,7 +522,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 						if (lane == 0) umma::mbar_arrive(&epi_done[b]);
 					}
 				}
-				merge_lanes(kd, kc, nd, nc, warp, __ballot_sync(0xffffffffu, cnt > 0), cnt, thr);
+				merge_lanes(kd, kc, nd, nc, warp, __ballot_sync(0xffffffffu, cnt > 0), cnt, thr, cap);
 			} else {
 				// staging warps: window of every candidate frame, then its chunks
 				const int pt = tid - 128, pw = pt >> 5;
@@ -621,7 +625,8 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 		if (selector) {
 			const long long g = s_g[tid];
 			if (g >= 0) {
-				const float root = kd[tid * kLs + kTop - 1];
+				// every dropped candidate's key was at least min(cap, 32nd kept key)
+				const float root = fminf(kd[tid * kLs + kTop - 1], a.thr0[g] - s_pn[tid]);
 				const bool skip = overflow || s_bad;
 				const float lbv = skip ? -1.f
 				                       : drop_bound(root + s_pn[tid], s_pn[tid], __int_as_float(s_qmax), s_dp[tid],
@@ -665,6 +670,84 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 	if (warp == 0) {
 		umma::fence_after_sync();
 		umma::tmem_dealloc(tmem, kTmemCols);
+	}
+}
+
+// Starting threshold of the pre-screen, per reference: the exact distances
+// (FP32, any order: only a threshold) of anchor candidates -- in every frame
+// of the temporal range the window's centre (the reference's position moved
+// along the flow, or the reference itself) and its four neighbours -- and
+// the kAnchorRank-th smallest of them, widened by 5 %.  Candidates above it
+// are unlikely to be among the nearest, so the pre-screen lists only those
+// below it (or below its 32nd smallest, when lower); the bound on the
+// dropped candidates accounts for it.  One warp per reference.
+constexpr int kAnchorRank = 20;
+
+struct AnchorArgs {
+	const Tile *tiles;
+	int ntiles;
+	const int *grid;
+	const uint32_t *traj;
+	int nfm;
+	long long G;
+	float *thr0;
+};
+
+template <int PX, int PT>
+__global__ void __launch_bounds__(256) anchor_kernel(Image src, StepParams sp, AnchorArgs a)
+{
+	constexpr int K = PX * PX * PT;
+	const int lane = threadIdx.x & 31;
+	const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+	const int hw = (sp.wx - 1) / 2;
+	for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); g < a.G; g += nw) {
+		const Tile T = a.tiles[tile_of(a.tiles, a.ntiles, g)];
+		int x, y, t, t0, t1;
+		group_position(T, a.grid, g, x, y, t);
+		temporal_range(sp, t, t0, t1);
+		const int nwt = t1 - t0 + 1;
+		float v[2];
+#pragma unroll
+		for (int rep = 0; rep < 2; rep++) {
+			const int ai = lane + 32 * rep;
+			v[rep] = __int_as_float(0x7f800000);
+			if (ai >= 5 * nwt) continue;
+			const int ii = ai / 5, o = ai % 5;
+			const uint32_t c = a.traj[g * a.nfm + ii];
+			const int cx = (int)(c & 0xffffu), cy = (int)(c >> 16);
+			const int shx = min(0, cx - hw) + max(0, cx + hw - T.w + PX);
+			const int shy = min(0, cy - hw) + max(0, cy + hw - T.h + PX);
+			const int rx0 = max(0, cx - hw - shx), ry0 = max(0, cy - hw - shy);
+			const int rx1 = min(T.w - PX, cx + hw - shx), ry1 = min(T.h - PX, cy + hw - shy);
+			if (rx1 < rx0 || ry1 < ry0) continue;
+			const int qx = min(max(cx + (o == 1) - (o == 2), rx0), rx1);
+			const int qy = min(max(cy + (o == 3) - (o == 4), ry0), ry1);
+			const int qt = visit_frame(ii, t, t1);
+			float acc = 0.f;
+#pragma unroll 16
+			for (int k = 0; k < K; k++) {
+				const int ht = k / (PX * PX), hy = (k / PX) % PX, hx = k % PX;
+				const float df = __ldg(src.p + src.at(T.ox + x + hx, T.oy + y + hy, t + ht, 0)) -
+				                 __ldg(src.p + src.at(T.ox + qx + hx, T.oy + qy + hy, qt + ht, 0));
+				acc = fmaf(df, df, acc);
+			}
+			v[rep] = acc;
+		}
+		// the kAnchorRank-th smallest (repeated warp minimum)
+		float kth = __int_as_float(0x7f800000);
+		for (int k = 0; k < kAnchorRank; k++) {
+			const float m = fminf(v[0], v[1]);
+			float w = m;
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) w = fminf(w, __shfl_xor_sync(0xffffffffu, w, o));
+			kth = w;
+			const unsigned holder = __ballot_sync(0xffffffffu, m == w);
+			if (lane == __ffs(holder) - 1) {
+				if (v[0] == w) v[0] = __int_as_float(0x7f800000);
+				else v[1] = __int_as_float(0x7f800000);
+			}
+		}
+		if (lane == 0) a.thr0[g] = kth * 1.05f + 1.f;
 	}
 }
 
@@ -797,10 +880,15 @@ __global__ void __launch_bounds__(256) rerank_kernel(Image src, StepParams sp, R
 }
 
 template <int PX, int PT>
-cudaError_t launch_tc_t(const Image &src, const StepParams &sp, const TcArgs &ta, const RerankArgs &ra, int nsm,
-                        cudaStream_t st)
+cudaError_t launch_tc_t(const Image &src, const StepParams &sp, const TcArgs &ta, const RerankArgs &ra,
+                        const AnchorArgs &aa, int nsm, cudaStream_t st)
 {
-	cudaError_t e = cudaFuncSetAttribute(search_tc_kernel<PX, PT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+	long long ab = (aa.G + 7) / 8;   // eight references (warps) per block
+	if (ab > (long long)nsm * 16) ab = (long long)nsm * 16;
+	if (ab > 0) anchor_kernel<PX, PT><<<(int)ab, 256, 0, st>>>(src, sp, aa);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	e = cudaFuncSetAttribute(search_tc_kernel<PX, PT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
 	if (e != cudaSuccess) return e;
 	const long long nb = ta.nblocks < nsm ? ta.nblocks : nsm;
 	if (nb > 0) search_tc_kernel<PX, PT><<<(int)nb, kThreads, kSmem, st>>>(src, sp, ta);
@@ -896,7 +984,7 @@ size_t tc_smem_bytes() { return (size_t)kSmem; }
 
 cudaError_t launch_search_tc(const Image &src, const Tile *tiles, int ntiles, const int *grid, const uint32_t *traj,
                              const StepParams &sp, const long long *blocks, long long nblocks, long long G,
-                             uint32_t *cand, float *lb, int *status, uint8_t *nsimp, uint32_t *idx,
+                             uint32_t *cand, float *lb, float *thr0, int *status, uint8_t *nsimp, uint32_t *idx,
                              uint32_t *fallback, unsigned *nfallback, unsigned *nuncertified, int certified, int nsm,
                              cudaStream_t st)
 {
@@ -912,6 +1000,15 @@ cudaError_t launch_search_tc(const Image &src, const Tile *tiles, int ntiles, co
 	ta.cand = cand;
 	ta.lb = lb;
 	ta.status = status;
+	ta.thr0 = thr0;
+	AnchorArgs aa;
+	aa.tiles = tiles;
+	aa.ntiles = ntiles;
+	aa.grid = grid;
+	aa.traj = traj;
+	aa.nfm = ta.nfm;
+	aa.G = G;
+	aa.thr0 = thr0;
 	RerankArgs ra;
 	ra.tiles = tiles;
 	ra.ntiles = ntiles;
@@ -927,7 +1024,7 @@ cudaError_t launch_search_tc(const Image &src, const Tile *tiles, int ntiles, co
 	ra.nfallback = nfallback;
 	ra.nuncertified = nuncertified;
 	ra.certified = certified;
-	return sp.px == 4 ? launch_tc_t<4, 4>(src, sp, ta, ra, nsm, st) : launch_tc_t<8, 1>(src, sp, ta, ra, nsm, st);
+	return sp.px == 4 ? launch_tc_t<4, 4>(src, sp, ta, ra, aa, nsm, st) : launch_tc_t<8, 1>(src, sp, ta, ra, aa, nsm, st);
 }
 
 cudaError_t tc_selftest(const uint16_t *A, const uint16_t *B, float *D, int *status, cudaStream_t st)
