@@ -61,7 +61,7 @@ constexpr int kK = 64;                // patch elements (MMA K, four k-steps of 
 constexpr int kThreads = 256;         // warps 0-3 select, warps 4-7 stage and issue
 constexpr int kTop = 32;              // approximate candidates kept per reference
 constexpr int kMaxWt = 16;            // candidate frames per reference on this path
-constexpr int kWinHalves = 23552;     // staged window capacity (FP16 values)
+constexpr int kWinHalves = 16384;     // staged window capacity (FP16 values)
 constexpr int kTmemCols = 512;        // two accumulators of kN columns
 constexpr uint32_t kWaitLimit = 1u << 22;   // mbarrier polls before giving up
 
@@ -77,7 +77,8 @@ constexpr int kOffKd = kOffQn + 2 * kN * 4;               // kept keys: 128 x kL
 constexpr int kOffKc = kOffKd + kRefs * kLs * 4;          // kept candidates
 constexpr int kOffNd = kOffKc + kRefs * kLs * 4;          // newcomer keys
 constexpr int kOffNc = kOffNd + kRefs * kLs * 4;          // newcomer candidates
-constexpr int kOffWt = kOffNc + kRefs * kLs * 4;          // windows: kMaxWt x 128 x short4
+constexpr int kOffDv = kOffNc + kRefs * kLs * 4;          // 4 warps x 32 lanes x 36 keys (one group)
+constexpr int kOffWt = kOffDv + 4 * 32 * 36 * 4;          // windows: kMaxWt x 128 x short4
 constexpr int kSmem = kOffWt + kMaxWt * kRefs * 8;
 
 static_assert(kSmem <= 227 * 1024, "shared memory");
@@ -246,6 +247,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 	float *nd = reinterpret_cast<float *>(sm + kOffNd);
 	uint32_t *nc = reinterpret_cast<uint32_t *>(sm + kOffNc);
 	short4 *wt = reinterpret_cast<short4 *>(sm + kOffWt);
+	float *dv = reinterpret_cast<float *>(sm + kOffDv);
 
 	// per operand buffer: MMA finished, norms written (staging warps), read out
 	// (selection warps)
@@ -448,6 +450,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 				float thr = cap < __int_as_float(0x7f800000) ? cap : __int_as_float(0x7f800000);
 				int cnt = 0;                               // newcomers waiting for a merge
 				const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+				float *mydv = dv + (warp * 32 + lane) * 36;
 				for (int ii = 0; ii < nwt; ii++) {
 					const Union u = uni[ii];
 					const int UW = u.x1 - u.x0 + 1, UH = u.y1 - u.y0 + 1;
@@ -500,21 +503,28 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 							hits &= wmask;
 							if (!__any_sync(0xffffffffu, hits)) continue;
 							// the hits join the reference's newcomers (candidate = frame << 16 |
-							// position in the frame's union); a list that would overflow is
-							// first merged into the kept 32 by the whole warp
-							const unsigned over = __ballot_sync(0xffffffffu, cnt + __popc(hits) > kTop);
-							if (over) merge_lanes(kd, kc, nd, nc, warp, over, cnt, thr, cap);
+							// position in the frame's union), one per lane and round; a full
+							// list is merged into the kept 32 by the whole warp
 							if (hits) {
-								const uint32_t cbase = ((uint32_t)ii << 16) | (uint32_t)g0c;
-								float *ndr = nd + r * kLs;
-								uint32_t *ncr = nc + r * kLs;
 #pragma unroll
-								for (int c = 0; c < 32; c++)
-									if ((hits >> c) & 1u) {
-										ndr[cnt] = key[c];
-										ncr[cnt] = cbase + (uint32_t)c;
+								for (int c4 = 0; c4 < 8; c4++)
+									*reinterpret_cast<float4 *>(mydv + 4 * c4) =
+										make_float4(key[4 * c4], key[4 * c4 + 1], key[4 * c4 + 2], key[4 * c4 + 3]);
+							}
+							const uint32_t cbase = ((uint32_t)ii << 16) | (uint32_t)g0c;
+							while (__any_sync(0xffffffffu, hits)) {
+								if (hits) {
+									const int c = __ffs(hits) - 1;
+									hits &= hits - 1u;
+									const float d = mydv[c];
+									if (d < thr) {
+										nd[r * kLs + cnt] = d;
+										nc[r * kLs + cnt] = cbase + (uint32_t)c;
 										cnt++;
 									}
+								}
+								const unsigned full = __ballot_sync(0xffffffffu, cnt == kTop);
+								if (full) merge_lanes(kd, kc, nd, nc, warp, full, cnt, thr, cap);
 							}
 						}
 						umma::fence_before_sync();
