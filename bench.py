@@ -480,7 +480,8 @@ def main():
     forms = {}
     import train_gains
     gains = train_gains.load_weights()
-    variants = [("mixed", {"mixed": True}), ("vbm3d_search", {"vbm3d": True}), ("paste_boost", {})]
+    variants = [("mixed", {"mixed": True}), ("mixed_certified", {"mixed": "certified"}),
+                ("vbm3d_search", {"vbm3d": True}), ("paste_boost", {})]
     if gains is not None:
         ctx.set_gain_network(gains)
         variants += [("learned", {"learned": True}), ("learned+mixed", {"learned": True, "mixed": True})]
@@ -492,7 +493,7 @@ def main():
         for _ in range(2):
             ctx.runNlBayes(d_nz, d_ff, d_bf, v1, v2, basic=d_basic, final=d_final, nparts=args.nparts, **kw)
         tms = []
-        for _ in range(args.steps):
+        for _ in range(max(2, min(args.steps, 5))):   # a few timed runs per form keep the bench short
             ctx.runNlBayes(d_nz, d_ff, d_bf, v1, v2, basic=d_basic, final=d_final, nparts=args.nparts, **kw)
             ms, _ = ctx.timings()
             tms.append(ms[4])
@@ -505,6 +506,10 @@ def main():
         if kw.get("learned"):
             g, fb = ctx.learned_stats()
             forms[name]["fallback_groups"] = [fb, g]
+        if kw.get("mixed"):
+            g, ex, unc = ctx.mixed_stats()
+            forms[name]["search_groups"] = {"tensor_core_prescreen": g, "exact_search": ex,
+                                            "uncertified_rerank": unc}
     line["forms"] = forms
     # the step before the path: TV-L1 flows of the whole video (2(F-1) frame
     # pairs in one batch, tvl1flow-seq.sh parameters), host video in, flows out

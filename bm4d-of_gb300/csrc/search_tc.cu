@@ -545,16 +545,16 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 					const int wh = UH + PX - 1, ww = UW + PX - 1;
 					// the previous frame's chunks are all built: the window can go
 					asm volatile("bar.sync 1, 128;" ::: "memory");
-					// eight rows per warp in flight: loads first, then conversions
+					// sixteen rows per warp in flight: loads first, then conversions
 					{
 						float em = 0.f;
 						const int nrow = PT * wh;
 						for (int x2 = lane; 2 * x2 < ww; x2 += 32) {
 							const bool two = 2 * x2 + 1 < ww;
-							for (int r0 = pw; r0 < nrow; r0 += 32) {
-								float v0[8], v1[8];
+							for (int r0 = pw; r0 < nrow; r0 += 64) {
+								float v0[16], v1[16];
 #pragma unroll
-								for (int k = 0; k < 8; k++) {
+								for (int k = 0; k < 16; k++) {
 									const int row = r0 + 4 * k;
 									v0[k] = v1[k] = 0.f;
 									if (row < nrow) {
@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(kThreads, 1) search_tc_kernel(Image src, StepP
 									}
 								}
 #pragma unroll
-								for (int k = 0; k < 8; k++) {
+								for (int k = 0; k < 16; k++) {
 									const int row = r0 + 4 * k;
 									if (row < nrow) {
 										const float a0 = v0[k] - centre, a1 = two ? v1[k] - centre : 0.f;
