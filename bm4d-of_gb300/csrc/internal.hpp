@@ -58,13 +58,6 @@ cudaError_t launch_search_vbm3d(const Image &src, const Image &ffl, const Image 
                                 int ntiles, const int *grid, const StepParams &sp, int reps, long long g_begin,
                                 long long g_end, uint8_t *nsimp, uint32_t *idx, int nsm, cudaStream_t st);
 
-// search_mixed.cu
-void mixed_blocks(const std::vector<Tile> &tiles, std::vector<long long> &out);
-bool mixed_supported(const StepParams &sp);
-cudaError_t launch_search_mixed(const Image &src, const Tile *tiles, int ntiles, const int *grid,
-                                const uint32_t *traj, const StepParams &sp, const long long *blocks,
-                                long long nblocks, uint8_t *nsimp, uint32_t *idx, int nsm, cudaStream_t st);
-
 // search_tc.cu: tensor-core pre-screen + certified exact re-rank; the groups
 // it cannot certify are listed for launch_search (list mode)
 void tc_blocks(const std::vector<Tile> &tiles, std::vector<long long> &out);

@@ -349,7 +349,6 @@ struct StepState {
 	Plan pl;
 	StepParams sp;
 	long long G = 0, chunk = 0;
-	bool mixed_search = false;   // FP16 mma.sync pre-screen (search_mixed.cu)
 	bool tc_search = false;      // tcgen05 pre-screen + certified re-rank (search_tc.cu)
 	size_t nblocks = 0;
 	PasteScratch paste = {nullptr, nullptr, nullptr, nullptr, nullptr};   // doPasteBoost only
@@ -500,10 +499,8 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	}
 	std::vector<float> win = make_window(p.agg_window != 0, sp.px, sp.pt);
 	S.tc_search = mode.mixed && tc_supported(sp, pl.tiles);
-	S.mixed_search = mode.mixed && !S.tc_search && mixed_supported(sp);
 	std::vector<long long> blocks;
 	if (S.tc_search) tc_blocks(pl.tiles, blocks);
-	else if (S.mixed_search) mixed_blocks(pl.tiles, blocks);
 	S.nblocks = blocks.size();
 
 	// host staging
@@ -544,7 +541,7 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	SBUF("small", 64 + ntiles, S.d_small);
 	SBUF("traj", (size_t)G * search_frames_max(sp), S.d_traj);
 	SBUF("edges", G, S.d_edges);   // a group switches off at most one other
-	if (S.mixed_search || S.tc_search) SBUF("mixed_blocks", blocks.size(), S.d_blocks);
+	if (S.tc_search) SBUF("tc_blocks", blocks.size(), S.d_blocks);
 	if (S.tc_search) {
 		SBUF("tc_cand", (size_t)G * 32, S.d_cand);
 		SBUF("tc_lb", G, S.d_lb);
@@ -615,7 +612,7 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 		CK(cudaMemcpyAsync(S.d_basis, S.h_stage + S.o_basis, nbasis, cudaMemcpyHostToDevice, st));
 		CK(cudaMemcpyAsync(S.d_binv, S.h_stage + S.o_binv, nbasis, cudaMemcpyHostToDevice, st));
 		CK(cudaMemcpyAsync(S.d_win, S.h_stage + S.o_win, sizeof(float) * sp.spc, cudaMemcpyHostToDevice, st));
-		if (S.mixed_search || S.tc_search)
+		if (S.tc_search)
 			CK(cudaMemcpyAsync(S.d_blocks, S.h_stage + S.o_blocks, sizeof(long long) * S.nblocks,
 			                   cudaMemcpyHostToDevice, st));
 		CK(cudaMemsetAsync(S.d_small, 0, sizeof(unsigned) * (64 + ntiles), st));
@@ -642,12 +639,6 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 			CK(launch_search(src, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, 0, G, S.d_nsimp, S.d_idx, nullptr,
 			                 ctx->nsm, st, S.d_fb, S.d_small + 4));
 			ctx->launches += 5;
-		} else if (S.mixed_search) {
-			// FP16 tensor-core pre-screen + exact re-rank of the best 2k
-			CK(launch_traj(ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp, G, S.d_traj, st));
-			CK(launch_search_mixed(on_noisy ? noisy : basic, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, S.d_blocks,
-			                       (long long)S.nblocks, S.d_nsimp, S.d_idx, ctx->nsm, st));
-			ctx->launches += 2;
 		} else {
 			CK(launch_traj(ffl, bfl, S.d_tiles, ntiles, S.d_grid, sp, G, S.d_traj, st));
 			CK(launch_search(on_noisy ? noisy : basic, S.d_tiles, ntiles, S.d_grid, S.d_traj, sp, 0, G, S.d_nsimp,
