@@ -445,7 +445,10 @@ def main():
     flops_per_launch = statistics.mean(g * 3 * 64 * ncand for g in groups)
     launch_ms = statistics.mean(searches) / 2.0
     achieved = flops_per_launch / (launch_ms / 1e3) / 1e12
-    peak = 152 * 128 * 2.07e9 / 1e12
+    # the search's instruction mix timed alone on this GPU (registers only,
+    # packed subtract and multiply, scalar adds): the rate it could reach
+    peak, mix_ms = bm4dof.fp32_mix_rate(local)
+    nominal = 152 * 128 * 2.07e9 / 1e12
     psnr = lambda a, b: float(10 * np.log10(255.0 ** 2 / np.mean((a.astype(np.float64) - b) ** 2)))
     final_np = d_final.cpu().numpy()
     line = {
@@ -462,8 +465,10 @@ def main():
                      "traffic_source": "ncu dram__bytes_read+write of search_kernel on 480x272x12, "
                                        "scaled by pixels (the frames and flows, read about once)",
                      "kernel": "search_kernel",
-                     "peak_source": "nominal FP32 CUDA-core rate: 152 SMs x 128 lanes x 2.07 GHz "
-                                    "(MEASURED_PEAKS.json has HBM and bf16 tensor peaks only)"},
+                     "peak_source": "measured on this GPU by bm4dof_fp32_mix_rate: the exact search's FP32 "
+                                    "instruction mix (packed sub/mul.rn.f32x2 + scalar adds) from registers, "
+                                    "3 ops per element (MEASURED_PEAKS.json has HBM and bf16 tensor peaks only)",
+                     "nominal_fp32_tops": nominal, "frac_of_nominal": achieved / nominal},
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(nz.nbytes + ff.nbytes + bf.nbytes),
                 "d2h_bytes_per_step": int(2 * nz.nbytes)},

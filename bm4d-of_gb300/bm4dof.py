@@ -45,7 +45,7 @@ EXPORTS = [
     "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run", "bm4dof_process",
     "bm4dof_set_memory_limit", "bm4dof_plan",
     "bm4dof_get_groups", "bm4dof_last_timings", "bm4dof_search_groups_noalloc",
-    "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_mixed_stats", "bm4dof_tc_selftest",
+    "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_mixed_stats", "bm4dof_tc_selftest", "bm4dof_fp32_mix_rate",
     "bm4dof_gain_samples",
     "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_params", "bm4dof_trainer_state",
     "bm4dof_trainer_grad",
@@ -195,6 +195,8 @@ def load(path: str = LIB_PATH):
     L.bm4dof_mixed_stats.restype = C.c_int
     L.bm4dof_tc_selftest.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.bm4dof_tc_selftest.restype = C.c_int
+    L.bm4dof_fp32_mix_rate.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.bm4dof_fp32_mix_rate.restype = C.c_int
     L.bm4dof_gain_samples.argtypes = [C.c_void_p] * 5 + [C.c_uint] * 3 + [
         C.POINTER(Params), C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
         C.POINTER(C.c_size_t)]
@@ -563,6 +565,14 @@ def tc_selftest(a, b):
     _check(load().bm4dof_tc_selftest(C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
                                      C.c_void_p(d.data_ptr()), C.c_void_p(stream)))
     return d
+
+
+def fp32_mix_rate(device=0):
+    """Measured FP32 rate (tera-operations/s, 3 per patch element) of the exact
+    search's instruction mix (bm4dof_fp32_mix_rate) and one launch's ms."""
+    t, ms = C.c_float(), C.c_float()
+    _check(load().bm4dof_fp32_mix_rate(device, C.byref(t), C.byref(ms)))
+    return t.value, ms.value
 
 
 def plan(W, H, F, params, nparts=2, crop=None, process=False):

@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 SOURCES = ["search.cu", "search_vbm3d.cu", "search_tc.cu", "filter.cu", "aggregate.cu", "runtime.cu", "noalloc.cu",
-           "mlp.cu", "learned.cu", "tvl1.cu",
+           "mlp.cu", "learned.cu", "tvl1.cu", "peaks.cu",
            "params.cpp", "basis.cpp"]
 
 

@@ -129,7 +129,12 @@ bm4dof_status bm4dof_set_memory_limit(bm4dof_ctx *ctx, size_t bytes);
 /* Flags for bm4dof_run. */
 #define BM4DOF_DEVICE_POINTERS  0x1u  /* all video pointers are device pointers  */
 #define BM4DOF_KEEP_GROUPS      0x2u  /* record neighbour lists for inspection   */
-#define BM4DOF_MIXED_PRECISION  0x4u  /* FP16 distance pre-screen + BF16 transforms */
+/* The patch search as a tensor-core pre-screen (tcgen05, FP16 patches, FP32
+ * accumulation) of the 32 best candidates per group, then their exact FP32
+ * distances, certified against a bound on every dropped candidate; the group
+ * filter stays FP32.  A certified group's neighbour list is the exact path's;
+ * see bm4dof_mixed_stats and BM4DOF_MIXED_CERTIFIED. */
+#define BM4DOF_MIXED_PRECISION  0x4u
 #define BM4DOF_LEARNED          0x8u  /* learned form: no step-1 pass (see below)  */
 /* The predictive patch search of the reference built with -DVBM3D_SEARCH
  * (src/core/nldct.cpp:892-1130, 1351-1589) instead of the exhaustive one:
@@ -362,6 +367,14 @@ bm4dof_status bm4dof_learned_stats(bm4dof_ctx *ctx, unsigned long long *groups,
  * other group's neighbour list is certified to be the exact path's. */
 bm4dof_status bm4dof_mixed_stats(bm4dof_ctx *ctx, unsigned long long *groups, unsigned long long *exact,
                                  unsigned long long *uncertified);
+
+/* No counterpart in the reference: the measured FP32 rate of the exact patch
+ * search's instruction mix on `device` (per two patch elements one packed
+ * subtract, one packed multiply and two scalar adds, the reference's
+ * separately rounded operations), in tera-operations per second counting 3
+ * per element -- the denominator of that kernel's roofline.  *ms (may be
+ * NULL) receives one launch's time.  Allocates a few bytes; synchronises. */
+bm4dof_status bm4dof_fp32_mix_rate(int device, float *tops, float *ms);
 
 /* No counterpart in the reference: a self-check of the tensor-core operand
  * layout.  d (128 x 256 floats, row-major) = a (128 x 64 FP16, row-major) times
