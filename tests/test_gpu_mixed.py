@@ -120,3 +120,23 @@ def test_mixed_unsupported_falls_back_to_exact(gpulib, gpuctx):
     a = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=2)
     b = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=2, mixed=True)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("sigma", [10.0, 20.0, 40.0])
+def test_mixed_rgb_video(gpulib, gpuctx, sigma):
+    # RGB video (the mixed-precision colour workload on a crop): step 1 searches
+    # the first opponent channel through the tensor-core pre-screen, step 2
+    # compares all three channels with the exact search
+    W, H, F = 128, 96, 8
+    clean, nz, ff, bf = video_case(W, H, F, sigma=sigma, seed=90, channels=3)
+    p = resolve_params(gpulib, (W, H, F, 3), sigma, **CFG_VIDEO)
+    pb, pf, pr = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=2, keep_groups=True)
+    plain = lists(gpuctx, 2)
+    cb, cf, cr = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=2, keep_groups=True, mixed="certified")
+    same_lists(plain, lists(gpuctx, 2))
+    assert np.array_equal(pb, cb) and np.array_equal(pf, cf)
+    mb, mf, mr = gpuctx.runNlBayes(nz, ff, bf, *p, nparts=2, keep_groups=True, mixed=True)
+    groups, exact, uncertified = gpuctx.mixed_stats()
+    assert groups > 0
+    assert set_agreement(plain[0], lists(gpuctx, 2)[0]) >= 0.995
+    assert abs(psnr(pf, clean) - psnr(mf, clean)) <= 0.01
