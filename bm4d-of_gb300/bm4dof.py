@@ -222,6 +222,15 @@ def load(path: str = LIB_PATH):
     return L
 
 
+def _out_array(a, shape):
+    """a itself when it is a writable C-contiguous float32 array of `shape`,
+    else a float32 copy of it (returned to the caller, as the outputs are)."""
+    if isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags["C_CONTIGUOUS"] and \
+            a.flags["WRITEABLE"] and a.shape == tuple(shape):
+        return a
+    return np.array(a, np.float32, copy=True).reshape(shape)
+
+
 def _mixed_flags(mixed):
     """mixed=True: the mixed-precision form; mixed="certified": the same with
     the exact path's neighbour lists (BM4DOF_MIXED_CERTIFIED)."""
@@ -364,9 +373,11 @@ class Context:
             F, Cc, H, W = noisy.shape
             ff = None if fflow is None else np.ascontiguousarray(fflow, np.float32)
             bf = None if bflow is None else np.ascontiguousarray(bflow, np.float32)
-            basic = np.zeros_like(noisy) if basic is None else np.array(basic, np.float32, copy=True)
-            if final is None:
-                final = np.zeros_like(noisy)
+            # basic is in/out as the reference's Video<float>& basic: the
+            # caller's array is written in place when it can take float32 data
+            # (so pinned host buffers stay the copy targets), else a copy is
+            basic = np.zeros_like(noisy) if basic is None else _out_array(basic, noisy.shape)
+            final = np.zeros_like(noisy) if final is None else _out_array(final, noisy.shape)
             ptr = lambda a: None if a is None else C.c_void_p(a.ctypes.data)
             args = (ptr(noisy), ptr(ff), ptr(bf), W, H, Cc, F, ptr(basic), ptr(final))
         ratios = (C.c_float * 2)()
