@@ -12,6 +12,7 @@ this module fails loudly when libbm4dof_gpu.so has not been built.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import json
 import os
@@ -42,12 +43,14 @@ STATUS = {
 EXPORTS = [
     "bm4dof_initialize_params", "bm4dof_set_size_search_window", "bm4dof_set_size_patch",
     "bm4dof_set_n_similar_patches", "bm4dof_format_params", "bm4dof_print_params",
-    "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_run", "bm4dof_process",
+    "bm4dof_last_error", "bm4dof_version", "bm4dof_create", "bm4dof_destroy", "bm4dof_get_stream", "bm4dof_run",
+    "bm4dof_process",
     "bm4dof_set_memory_limit", "bm4dof_plan",
     "bm4dof_get_groups", "bm4dof_last_timings", "bm4dof_search_groups_noalloc",
     "bm4dof_set_gain_network", "bm4dof_learned_stats", "bm4dof_mixed_stats", "bm4dof_tc_selftest", "bm4dof_fp32_mix_rate",
     "bm4dof_gain_samples",
-    "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_params", "bm4dof_trainer_state",
+    "bm4dof_trainer_create", "bm4dof_trainer_destroy", "bm4dof_trainer_get_stream", "bm4dof_trainer_params",
+    "bm4dof_trainer_state",
     "bm4dof_trainer_grad",
     "bm4dof_trainer_step", "bm4dof_trainer_predict", "bm4dof_run_batched", "bm4dof_autotune",
     "bm4dof_tvl1_default_params", "bm4dof_tvl1_pairs", "bm4dof_tvl1_video",
@@ -151,6 +154,8 @@ def load(path: str = LIB_PATH):
     L.bm4dof_create.restype = C.c_int
     L.bm4dof_destroy.argtypes = [C.c_void_p]
     L.bm4dof_destroy.restype = None
+    L.bm4dof_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    L.bm4dof_get_stream.restype = C.c_int
     L.bm4dof_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint, C.c_uint, C.c_uint,
                              C.c_uint, C.c_void_p, C.c_void_p, C.POINTER(Params), C.POINTER(Params),
                              C.c_uint, C.c_uint, C.POINTER(C.c_float)]
@@ -205,6 +210,8 @@ def load(path: str = LIB_PATH):
     L.bm4dof_trainer_create.restype = C.c_int
     L.bm4dof_trainer_destroy.argtypes = [C.c_void_p]
     L.bm4dof_trainer_destroy.restype = None
+    L.bm4dof_trainer_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    L.bm4dof_trainer_get_stream.restype = C.c_int
     L.bm4dof_trainer_params.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
     L.bm4dof_trainer_params.restype = C.c_int
     L.bm4dof_trainer_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
@@ -323,6 +330,26 @@ def _is_cuda_tensor(x):
     return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
 
 
+@contextlib.contextmanager
+def _stream_order(get_stream, handle, device):
+    """Orders the library's own stream (bm4dof_get_stream,
+    bm4dof_trainer_get_stream) after torch's current stream on entry, and
+    torch's current stream after it on exit, so that CUDA tensors torch has
+    just written are complete before the library reads them, and memory that
+    torch frees after the call is not reused while the library still reads
+    it.  Neither side waits on the host."""
+    import torch
+    s = C.c_void_p()
+    _check(get_stream(handle, C.byref(s)))
+    cur = torch.cuda.current_stream(device)
+    lib = torch.cuda.ExternalStream(s.value, device=device)
+    lib.wait_stream(cur)
+    try:
+        yield
+    finally:
+        cur.wait_stream(lib)
+
+
 class Context:
     """A device context (one CUDA device, one stream) -- wraps bm4dof_create."""
 
@@ -335,6 +362,9 @@ class Context:
         if self._h:
             load().bm4dof_destroy(self._h)
             self._h = C.c_void_p()
+
+    def _ordered(self):
+        return _stream_order(load().bm4dof_get_stream, self._h, self.device)
 
     def __del__(self):
         try:
@@ -381,7 +411,11 @@ class Context:
             ptr = lambda a: None if a is None else C.c_void_p(a.ctypes.data)
             args = (ptr(noisy), ptr(ff), ptr(bf), W, H, Cc, F, ptr(basic), ptr(final))
         ratios = (C.c_float * 2)()
-        _check(load().bm4dof_run(self._h, *args, C.byref(p1), C.byref(p2), nparts, flags, ratios))
+        if flags & DEVICE_POINTERS:
+            with self._ordered():
+                _check(load().bm4dof_run(self._h, *args, C.byref(p1), C.byref(p2), nparts, flags, ratios))
+        else:
+            _check(load().bm4dof_run(self._h, *args, C.byref(p1), C.byref(p2), nparts, flags, ratios))
         return basic, final, (ratios[0], ratios[1])
 
     def groups(self, step, tile, stride=32):
@@ -420,7 +454,9 @@ class Context:
         t = None
         if tuning is not None:
             t = Tuning(**tuning) if isinstance(tuning, dict) else tuning
-        _check(load().bm4dof_run_batched(self._h, arr, len(items), flags, C.byref(t) if t is not None else None))
+        with self._ordered():
+            _check(load().bm4dof_run_batched(self._h, arr, len(items), flags,
+                                             C.byref(t) if t is not None else None))
         return [(q.ratios[0], q.ratios[1]) for q in arr]
 
     def autotune(self, items, sample=16, mixed=False, learned=False, vbm3d=False):
@@ -430,8 +466,9 @@ class Context:
         best = Tuning()
         table = (C.c_float * (4 * 32))()
         rows = C.c_uint()
-        _check(load().bm4dof_autotune(self._h, arr, len(items), sample, flags, C.byref(best), table, 32,
-                                      C.byref(rows)))
+        with self._ordered():
+            _check(load().bm4dof_autotune(self._h, arr, len(items), sample, flags, C.byref(best), table, 32,
+                                          C.byref(rows)))
         tab = [tuple(table[4 * i:4 * i + 4]) for i in range(min(rows.value, 32))]
         return best.as_dict(), tab
 
@@ -473,9 +510,11 @@ class Context:
             tgt = torch.empty((cap, 64), dtype=torch.float32, device=dev)
             valid = torch.empty((cap,), dtype=torch.uint8, device=dev)
             ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
-            code = L.bm4dof_gain_samples(self._h, ptr(noisy.contiguous()), ptr(basic.contiguous()),
-                                         ptr(fflow), ptr(bflow), W, H, F, C.byref(p2), nparts,
-                                         DEVICE_POINTERS, ptr(feat), ptr(tgt), ptr(valid), cap, C.byref(n))
+            nz, bs = noisy.contiguous(), basic.contiguous()
+            with self._ordered():
+                code = L.bm4dof_gain_samples(self._h, ptr(nz), ptr(bs), ptr(fflow), ptr(bflow), W, H, F,
+                                             C.byref(p2), nparts, DEVICE_POINTERS, ptr(feat), ptr(tgt),
+                                             ptr(valid), cap, C.byref(n))
             if code == 1 and n.value > cap:
                 cap = n.value
                 continue
@@ -626,6 +665,10 @@ class Trainer:
         self._h = C.c_void_p()
         _check(load().bm4dof_trainer_create(C.byref(self._h), device, batch, seed))
         self.batch = batch
+        self.device = device
+
+    def _ordered(self):
+        return _stream_order(load().bm4dof_trainer_get_stream, self._h, self.device)
 
     def close(self):
         if self._h:
@@ -678,23 +721,27 @@ class Trainer:
     def grad(self, feat, target):
         g = np.zeros(GAIN_PARAMS, np.float32)
         loss = C.c_float()
-        _check(load().bm4dof_trainer_grad(self._h, C.c_void_p(feat.data_ptr()), C.c_void_p(target.data_ptr()),
-                                          feat.shape[0], C.c_void_p(g.ctypes.data), C.byref(loss)))
+        with self._ordered():
+            _check(load().bm4dof_trainer_grad(self._h, C.c_void_p(feat.data_ptr()), C.c_void_p(target.data_ptr()),
+                                              feat.shape[0], C.c_void_p(g.ctypes.data), C.byref(loss)))
         return g, loss.value
 
     def step(self, feat, target, lr=1e-3, weight_decay=1e-4, want_loss=True):
         """One AdamW step; returns the batch loss (before the update) when
         want_loss, else None (no host synchronisation)."""
         loss = C.c_float()
-        _check(load().bm4dof_trainer_step(self._h, C.c_void_p(feat.data_ptr()), C.c_void_p(target.data_ptr()),
-                                          feat.shape[0], lr, weight_decay, C.byref(loss) if want_loss else None))
+        with self._ordered():
+            _check(load().bm4dof_trainer_step(self._h, C.c_void_p(feat.data_ptr()), C.c_void_p(target.data_ptr()),
+                                              feat.shape[0], lr, weight_decay,
+                                              C.byref(loss) if want_loss else None))
         return loss.value if want_loss else None
 
     def predict(self, feat):
         import torch
         out = torch.empty((feat.shape[0], 64), dtype=torch.float32, device=feat.device)
-        _check(load().bm4dof_trainer_predict(self._h, C.c_void_p(feat.data_ptr()), feat.shape[0],
-                                             C.c_void_p(out.data_ptr())))
+        with self._ordered():
+            _check(load().bm4dof_trainer_predict(self._h, C.c_void_p(feat.data_ptr()), feat.shape[0],
+                                                 C.c_void_p(out.data_ptr())))
         return out
 
 

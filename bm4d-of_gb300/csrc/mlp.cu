@@ -525,6 +525,14 @@ bm4dof_status bm4dof_trainer_create(bm4dof_trainer **out, int device, unsigned b
 	return BM4DOF_OK;
 }
 
+bm4dof_status bm4dof_trainer_get_stream(bm4dof_trainer *t, void **stream)
+{
+	clear_error();
+	if (!t || !stream) { set_error("bm4dof_trainer_get_stream: null argument"); return BM4DOF_ERR_ARGUMENT; }
+	*stream = static_cast<void *>(t->st);
+	return BM4DOF_OK;
+}
+
 void bm4dof_trainer_destroy(bm4dof_trainer *t)
 {
 	if (!t) return;

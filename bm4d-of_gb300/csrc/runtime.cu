@@ -897,6 +897,14 @@ bm4dof_status bm4dof_create(bm4dof_ctx **out, int device)
 	return BM4DOF_OK;
 }
 
+bm4dof_status bm4dof_get_stream(bm4dof_ctx *ctx, void **stream)
+{
+	clear_error();
+	if (!ctx || !stream) { set_error("bm4dof_get_stream: null argument"); return BM4DOF_ERR_ARGUMENT; }
+	*stream = static_cast<void *>(ctx->st);
+	return BM4DOF_OK;
+}
+
 void bm4dof_destroy(bm4dof_ctx *ctx)
 {
 	if (!ctx) return;

@@ -119,6 +119,14 @@ typedef struct bm4dof_ctx bm4dof_ctx;
 bm4dof_status bm4dof_create(bm4dof_ctx **ctx, int device);
 void          bm4dof_destroy(bm4dof_ctx *ctx);
 
+/* The context's stream (a cudaStream_t, created non-blocking): every call on
+ * the context runs its device work there.  Device inputs written by work on
+ * another stream must be ordered before the call by the caller (an event
+ * recorded on its stream and cudaStreamWaitEvent on this one), and work of
+ * the caller's stream that reads the outputs or reuses the inputs' memory
+ * after it (the reverse wait). */
+bm4dof_status bm4dof_get_stream(bm4dof_ctx *ctx, void **stream);
+
 /* Caps the device memory the context's buffers may hold (0: no cap, the
  * default).  A call that would need more fails with BM4DOF_ERR_NO_MEMORY and
  * a message naming the buffer; the context stays usable.  The chunk budget of
@@ -409,6 +417,10 @@ bm4dof_status bm4dof_gain_samples(bm4dof_ctx *ctx, const float *noisy, const flo
 typedef struct bm4dof_trainer bm4dof_trainer;
 bm4dof_status bm4dof_trainer_create(bm4dof_trainer **t, int device, unsigned batch, unsigned seed);
 void          bm4dof_trainer_destroy(bm4dof_trainer *t);
+/* The trainer's own non-blocking stream, ordered against the caller's streams
+ * by the caller as for bm4dof_get_stream: bm4dof_trainer_step returns before
+ * its kernels have read feat and target unless it reports the loss. */
+bm4dof_status bm4dof_trainer_get_stream(bm4dof_trainer *t, void **stream);
 /* Reads (set = 0) or writes (set = 1) the FP32 master parameters as a host blob. */
 bm4dof_status bm4dof_trainer_params(bm4dof_trainer *t, float *params, size_t n, int set);
 /* Reads (set = 0) or writes (set = 1) the AdamW state for a checkpoint: the

@@ -47,8 +47,9 @@ def layer(gpulib, tmp_path_factory):
 
 @pytest.fixture(scope="module")
 def layer_ref(gpulib, reference, tmp_path_factory):
+    import __graft_entry__
     import pyoracle
-    root = pyoracle.ref_root()
+    root = __graft_entry__.reference_tree()
     if root is None:
         pytest.skip("REF_ROOT (the reference's source tree) not set")
     inc = ["-fopenmp", "-I" + os.path.join(ORACLE, "ref_stubs"), "-I" + os.path.join(root, "src", "core"),
