@@ -432,6 +432,7 @@ def main():
         ms, _ = step_host()
         e2e_ms.append(ms[4])
     barrier()
+    e2e_stage = ms
     e2e_value = world * mpf / (replica_max_ms(statistics.mean(e2e_ms), world) / 1e3)
 
     if rank != 0:
@@ -471,7 +472,9 @@ def main():
                      "nominal_fp32_tops": nominal, "frac_of_nominal": achieved / nominal},
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(nz.nbytes + ff.nbytes + bf.nbytes),
-                "d2h_bytes_per_step": int(2 * nz.nbytes)},
+                "d2h_bytes_per_step": int(2 * nz.nbytes),
+                "stage_ms": {"search": e2e_stage[0], "filter": e2e_stage[1], "aggregation": e2e_stage[2],
+                             "other": e2e_stage[3], "total": e2e_stage[4]}},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "stage_ms": {"search": stage_ms[0], "filter": stage_ms[1], "aggregation": stage_ms[2],

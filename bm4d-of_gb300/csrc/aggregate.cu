@@ -538,6 +538,276 @@ gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *_
 	}
 }
 
+// ---------------------------------------------------------------------------
+// Quad path (4x4 patches): one thread per quad of 4 horizontally adjacent
+// pixels.  A member patch whose origin lies in row oy and column ox covers
+// quads (ox+3)/4 and ox/4 (one quad when ox is a multiple of 4), so a
+// quad's list holds about 7/16 of the entries of its four pixels' lists, and
+// the four pixels' terms of one member row sit in one 32-byte sector that a
+// single thread reads.  Lists are indexed by quad position
+// ((to - t_lo) * h + y) * nq + q over the chunk's origin frames [t_lo, t_hi].
+// ---------------------------------------------------------------------------
+constexpr int kQuad = 4;
+
+// row lists: for quad q, origin row oy and origin frame to, the slots whose
+// origin column lies in [4q-3, 4q+3], merged into slot order.  The origin
+// lists of consecutive columns are consecutive in `list`, so the count is one
+// difference of offsets.  Entry = slot << 3 | (ox - 4q + 3).
+__global__ void rlist_count_kernel(int w, int h, int nq, int t_lo, int nf, const unsigned *__restrict__ off,
+                                   unsigned *__restrict__ cnt)
+{
+	const size_t n = (size_t)nq * h * nf;
+	for (size_t pos = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pos < n;
+	     pos += (size_t)gridDim.x * blockDim.x) {
+		const int q = (int)(pos % nq), oy = (int)((pos / nq) % h), to = t_lo + (int)(pos / ((size_t)nq * h));
+		const int lo = max(0, kQuad * q - 3), hi = min(w - kQuad, kQuad * q + 3);
+		unsigned c = 0;
+		if (oy <= h - kQuad && lo <= hi) {
+			const size_t base = ((size_t)to * h + oy) * w;
+			c = off[base + hi + 1] - off[base + lo];
+		}
+		cnt[pos] = c;
+	}
+}
+
+__global__ void rlist_build_kernel(int w, int h, int nq, int t_lo, int nf, const unsigned *__restrict__ off,
+                                   const unsigned *__restrict__ list, const unsigned *__restrict__ roff,
+                                   unsigned *__restrict__ rl)
+{
+	constexpr int L = 2 * kQuad - 1;
+	const size_t n = (size_t)nq * h * nf;
+	for (size_t pos = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pos < n;
+	     pos += (size_t)gridDim.x * blockDim.x) {
+		unsigned o = roff[pos];
+		if (roff[pos + 1] == o) continue;
+		const int q = (int)(pos % nq), oy = (int)((pos / nq) % h), to = t_lo + (int)(pos / ((size_t)nq * h));
+		const size_t base = ((size_t)to * h + oy) * w;
+		unsigned cur[L], end[L], head[L];
+#pragma unroll
+		for (int l = 0; l < L; l++) {
+			const int ox = kQuad * q - 3 + l;
+			cur[l] = end[l] = 0;
+			if (ox >= 0 && ox <= w - kQuad) {
+				cur[l] = off[base + ox];
+				end[l] = off[base + ox + 1];
+			}
+			head[l] = cur[l] < end[l] ? list[cur[l]] : 0xffffffffu;
+		}
+		for (;;) {
+			unsigned best = 0xffffffffu;
+			int bl = -1;
+#pragma unroll
+			for (int l = 0; l < L; l++)
+				if (head[l] < best) { best = head[l]; bl = l; }
+			if (bl < 0) break;
+			rl[o++] = best << 3 | (unsigned)bl;
+#pragma unroll
+			for (int l = 0; l < L; l++)
+				if (l == bl) head[l] = ++cur[l] < end[l] ? list[cur[l]] : 0xffffffffu;
+		}
+	}
+}
+
+// quad lists: for quad q, pixel row y and origin frame to, the row lists of
+// origin rows y-3..y merged into slot order.  Entry = slot << 5 | dy << 3 |
+// (ox - 4q + 3), dy = y - oy.
+__global__ void qlist_count_kernel(int h, int nq, int nf, const unsigned *__restrict__ roff,
+                                   unsigned *__restrict__ cnt)
+{
+	const size_t n = (size_t)nq * h * nf;
+	for (size_t pos = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pos < n;
+	     pos += (size_t)gridDim.x * blockDim.x) {
+		const int y = (int)((pos / nq) % h);
+		unsigned c = 0;
+#pragma unroll
+		for (int dy = 0; dy < kQuad; dy++) {
+			const int oy = y - dy;
+			if (oy < 0 || oy > h - kQuad) continue;
+			const size_t r = pos - (size_t)dy * nq;
+			c += roff[r + 1] - roff[r];
+		}
+		cnt[pos] = c;
+	}
+}
+
+__global__ void qlist_build_kernel(int h, int nq, int nf, const unsigned *__restrict__ roff,
+                                   const unsigned *__restrict__ rl, const unsigned *__restrict__ qoff,
+                                   unsigned *__restrict__ ql)
+{
+	const size_t n = (size_t)nq * h * nf;
+	for (size_t pos = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pos < n;
+	     pos += (size_t)gridDim.x * blockDim.x) {
+		unsigned o = qoff[pos];
+		if (qoff[pos + 1] == o) continue;
+		const int y = (int)((pos / nq) % h);
+		unsigned cur[kQuad], end[kQuad], head[kQuad];
+#pragma unroll
+		for (int dy = 0; dy < kQuad; dy++) {
+			const int oy = y - dy;
+			cur[dy] = end[dy] = 0;
+			if (oy >= 0 && oy <= h - kQuad) {
+				const size_t r = pos - (size_t)dy * nq;
+				cur[dy] = roff[r];
+				end[dy] = roff[r + 1];
+			}
+			head[dy] = cur[dy] < end[dy] ? rl[cur[dy]] : 0xffffffffu;
+		}
+		for (;;) {
+			unsigned best = 0xffffffffu;
+			int bl = -1;
+#pragma unroll
+			for (int l = 0; l < kQuad; l++)
+				if (head[l] < best) { best = head[l]; bl = l; }
+			if (bl < 0) break;
+			ql[o++] = (best >> 3) << 5 | (unsigned)bl << 3 | (best & 7u);
+#pragma unroll
+			for (int l = 0; l < kQuad; l++)
+				if (l == bl) head[l] = ++cur[l] < end[l] ? rl[cur[l]] : 0xffffffffu;
+		}
+	}
+}
+
+// Ordered gather, quad path: each thread merges the quad lists of the pt
+// origin frames covering its four pixels and adds each member's terms in
+// slot order, the order of the reference's scatter loop for every pixel.  A
+// member adds to the pixels j of the quad with 0 <= j - s < 4 (s = ox - 4q),
+// from element dx = j - s of its row.  Members are fetched D ahead of the one
+// being added (a register ring consumed in fetch order), so that up to 4*D
+// term loads of a thread are in flight.
+template <int PT, int CC>
+__global__ void __launch_bounds__(128)
+gather_quad_kernel(Tile T, StepParams sp, int t_lo, int t_hi, int f_hi, int nq, const unsigned *__restrict__ qoff,
+                   const unsigned *__restrict__ ql, const float *__restrict__ vals, float *__restrict__ acc,
+                   float *__restrict__ wacc)
+{
+	constexpr int TS = CC == 1 ? 2 : (CC <= 3 ? 4 : 8);
+	constexpr int D = CC == 1 ? 4 : 2;
+	const int w = T.w, h = T.h, spc = sp.spc;
+	const size_t wh = (size_t)w * h, plane = (size_t)nq * h;
+	const size_t n = plane * (size_t)(f_hi - t_lo + 1);
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+		const int t = t_lo + (int)(i / plane);
+		const size_t r = i % plane;
+		const int y = (int)(r / nq), q = (int)(r % nq);
+		unsigned cur[PT], end[PT], head[PT], nxt[PT];
+		bool any = false;
+#pragma unroll
+		for (int dt = 0; dt < PT; dt++) {
+			head[dt] = nxt[dt] = 0xffffffffu;
+			cur[dt] = end[dt] = 0;
+			const int to = t - dt;
+			if (to >= t_lo && to <= t_hi) {
+				const size_t qp = ((size_t)(to - t_lo) * h + y) * nq + q;
+				cur[dt] = qoff[qp];
+				end[dt] = qoff[qp + 1];
+				if (cur[dt] < end[dt]) {
+					head[dt] = __ldg(ql + cur[dt]);
+					any = true;
+					if (cur[dt] + 1 < end[dt]) nxt[dt] = __ldg(ql + cur[dt] + 1);
+				}
+			}
+		}
+		if (!any) continue;
+		const int x0 = kQuad * q;
+		const size_t pix = (size_t)t * wh + (size_t)y * w + x0;
+		float a[kQuad][CC], wa[kQuad];
+#pragma unroll
+		for (int j = 0; j < kQuad; j++) {
+			const bool in = x0 + j < w;
+#pragma unroll
+			for (int c = 0; c < CC; c++) a[j][c] = in ? acc[((size_t)t * CC + c) * wh + (size_t)y * w + x0 + j] : 0.f;
+			wa[j] = in ? wacc[pix + j] : 0.f;
+		}
+		auto fetch = [&](float (&x)[kQuad][TS], unsigned &m) -> bool {
+			unsigned best = 0xffffffffu;
+			int bl = -1;
+#pragma unroll
+			for (int l = 0; l < PT; l++)
+				if (head[l] < best) { best = head[l]; bl = l; }
+			if (bl < 0) return false;
+			const unsigned slot = best >> 5;
+			const int dy = (best >> 3) & 3, s = (int)(best & 7u) - 3;
+			const float *row = vals + ((size_t)slot * spc + (bl * kQuad + dy) * kQuad) * TS;
+			m = 0;
+#pragma unroll
+			for (int j = 0; j < kQuad; j++) {
+				const int dx = j - s;
+				if ((unsigned)dx < (unsigned)kQuad) {
+					m |= 1u << j;
+					if (TS == 2) {
+						const float2 v = __ldg(reinterpret_cast<const float2 *>(row + dx * TS));
+						x[j][0] = v.x;
+						x[j][1] = v.y;
+					} else {
+#pragma unroll
+						for (int k = 0; k < TS / 4; k++) {
+							const float4 v = __ldg(reinterpret_cast<const float4 *>(row + dx * TS) + k);
+							x[j][4 * k] = v.x;
+							x[j][4 * k + 1] = v.y;
+							x[j][4 * k + 2] = v.z;
+							x[j][4 * k + 3] = v.w;
+						}
+					}
+				}
+			}
+#pragma unroll
+			for (int l = 0; l < PT; l++)
+				if (l == bl) {
+					head[l] = nxt[l];
+					cur[l]++;
+					nxt[l] = cur[l] + 1 < end[l] ? __ldg(ql + cur[l] + 1) : 0xffffffffu;
+				}
+			return true;
+		};
+		float x[D][kQuad][TS];
+		unsigned m[D];
+		bool ok[D];
+#pragma unroll
+		for (int d = 0; d < D; d++) ok[d] = fetch(x[d], m[d]);
+		bool live = true;
+		while (live) {
+#pragma unroll
+			for (int d = 0; d < D; d++) {
+				if (live && !ok[d]) live = false;
+				if (live) {
+#pragma unroll
+					for (int j = 0; j < kQuad; j++)
+						if (m[d] >> j & 1u) {
+#pragma unroll
+							for (int c = 0; c < CC; c++) a[j][c] = __fadd_rn(a[j][c], x[d][j][c]);
+							wa[j] = __fadd_rn(wa[j], x[d][j][CC]);   // w * window[p], as the reference forms it
+						}
+					ok[d] = fetch(x[d], m[d]);
+				}
+			}
+		}
+#pragma unroll
+		for (int j = 0; j < kQuad; j++)
+			if (x0 + j < w) {
+#pragma unroll
+				for (int c = 0; c < CC; c++) acc[((size_t)t * CC + c) * wh + (size_t)y * w + x0 + j] = a[j][c];
+				wacc[pix + j] = wa[j];
+			}
+	}
+}
+
+template <int CC>
+void gather_quad_pt(int gb, cudaStream_t st, const Tile &T, const StepParams &sp, int t_lo, int t_hi, int f_hi,
+                    int nq, const unsigned *qoff, const unsigned *ql, const float *vals, float *acc, float *wacc)
+{
+	switch (sp.pt) {
+	case 1:
+		gather_quad_kernel<1, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
+		break;
+	case 2:
+		gather_quad_kernel<2, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
+		break;
+	default:
+		gather_quad_kernel<4, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
+		break;
+	}
+}
+
 template <int CC>
 void gather_pt(int gb, cudaStream_t st, const Tile &T, const StepParams &sp, int t_lo, int f_hi,
                const unsigned *soff, const unsigned *sl, const float *vals, float *acc, float *wacc)
@@ -690,6 +960,13 @@ cudaError_t launch_count_alive(const Tile *tiles, int ntiles, long long G, const
 	return cudaGetLastError();
 }
 
+// Kernels exclusive_scan launches for n entries.
+unsigned scan_kernels(size_t n)
+{
+	const size_t nb = (n + 1 + kScanBlock - 1) / kScanBlock;
+	return nb > 1 ? 2 + scan_kernels(nb - 1) : 1;
+}
+
 // Exclusive scan of data[0..n) in place; data[n] receives the total.
 cudaError_t exclusive_scan(unsigned *data, size_t n, unsigned *scratch, cudaStream_t st)
 {
@@ -706,8 +983,9 @@ cudaError_t exclusive_scan(unsigned *data, size_t n, unsigned *scratch, cudaStre
 
 cudaError_t launch_lists(long long ga, long long gb, int np, const uint8_t *nsimp, const uint32_t *idx,
                          const uint8_t *alive, size_t npos, unsigned *cnt, unsigned *off, unsigned *list,
-                         unsigned *scratch, cudaStream_t st)
+                         unsigned *scratch, unsigned *launches, cudaStream_t st)
 {
+	*launches += 3 + scan_kernels(npos);
 	cudaError_t e = cudaMemsetAsync(off, 0, (npos + 1) * sizeof(unsigned), st);
 	if (e != cudaSuccess) return e;
 	const long long ns = (gb - ga) * np;
@@ -721,15 +999,52 @@ cudaError_t launch_lists(long long ga, long long gb, int np, const uint8_t *nsim
 	return cudaGetLastError();
 }
 
+bool quad_path(const StepParams &sp)
+{
+	return sp.px == kQuad && (sp.pt == 1 || sp.pt == 2 || sp.pt == 4);
+}
+
+int list_entries_per_member(const StepParams &sp)
+{
+	// quad path: at most 2 row-list and 8 quad-list entries per member
+	return quad_path(sp) ? 10 : sp.px * sp.px;
+}
+
 cudaError_t launch_gather(const Tile &T, const StepParams &sp, int t_lo, int t_hi, const unsigned *off,
-                          const unsigned *list, unsigned *soff, unsigned *sl, unsigned *scratch,
-                          const float *vals, float *acc, float *wacc, cudaStream_t st)
+                          const unsigned *list, unsigned *cnt, unsigned *soff, unsigned *sl, size_t members,
+                          unsigned *scratch, const float *vals, float *acc, float *wacc, unsigned *launches,
+                          cudaStream_t st)
 {
 	// origin frames [t_lo, t_hi] hold the chunk's member patches; pixels of
 	// frames [t_lo, t_hi + pt - 1] receive them
 	if (t_hi < t_lo) return cudaSuccess;
+	const int f_hi = t_hi + sp.pt - 1 < sp.F - 1 ? t_hi + sp.pt - 1 : sp.F - 1;
+	if (quad_path(sp)) {
+		// row-list offsets in cnt (free once the origin lists are sorted), row
+		// lists then quad lists in sl
+		const int nq = (T.w + kQuad - 1) / kQuad, nf = t_hi - t_lo + 1;
+		const size_t nqp = (size_t)nq * T.h * nf;
+		const int b = grid_for((long long)nqp, 256, 16384);
+		unsigned *roff = cnt, *rl = sl, *ql = sl + 2 * members;
+		*launches += 5 + 2 * scan_kernels(nqp);
+		rlist_count_kernel<<<b, 256, 0, st>>>(T.w, T.h, nq, t_lo, nf, off, roff);
+		cudaError_t e = exclusive_scan(roff, nqp, scratch, st);
+		if (e != cudaSuccess) return e;
+		rlist_build_kernel<<<b, 256, 0, st>>>(T.w, T.h, nq, t_lo, nf, off, list, roff, rl);
+		qlist_count_kernel<<<b, 256, 0, st>>>(T.h, nq, nf, roff, soff);
+		e = exclusive_scan(soff, nqp, scratch, st);
+		if (e != cudaSuccess) return e;
+		qlist_build_kernel<<<b, 256, 0, st>>>(T.h, nq, nf, roff, rl, soff, ql);
+		const long long nthr = (long long)nq * T.h * (f_hi - t_lo + 1);
+		const int gb = grid_for(nthr, 128, 65535);
+		if (sp.C == 1) gather_quad_pt<1>(gb, st, T, sp, t_lo, t_hi, f_hi, nq, soff, ql, vals, acc, wacc);
+		else if (sp.C == 3) gather_quad_pt<3>(gb, st, T, sp, t_lo, t_hi, f_hi, nq, soff, ql, vals, acc, wacc);
+		else gather_quad_pt<4>(gb, st, T, sp, t_lo, t_hi, f_hi, nq, soff, ql, vals, acc, wacc);
+		return cudaGetLastError();
+	}
 	const size_t npos = (size_t)T.w * T.h * sp.F;
 	const int b = grid_for((long long)npos, 256, 16384);
+	*launches += 3 + scan_kernels(npos);
 	slist_count_kernel<<<b, 256, 0, st>>>(T.w, T.h, sp.F, sp.px, sp.pt, t_lo, t_hi, off, soff);
 	cudaError_t e = exclusive_scan(soff, npos, scratch, st);
 	if (e != cudaSuccess) return e;
@@ -737,7 +1052,6 @@ cudaError_t launch_gather(const Tile &T, const StepParams &sp, int t_lo, int t_h
 		slist_build_kernel<4><<<b, 256, 0, st>>>(T.w, T.h, sp.F, sp.px, sp.pt, t_lo, t_hi, off, list, soff, sl);
 	else
 		slist_build_kernel<0><<<b, 256, 0, st>>>(T.w, T.h, sp.F, sp.px, sp.pt, t_lo, t_hi, off, list, soff, sl);
-	const int f_hi = t_hi + sp.pt - 1 < sp.F - 1 ? t_hi + sp.pt - 1 : sp.F - 1;
 	const long long npix = (long long)T.w * T.h * (f_hi - t_lo + 1);
 	const int gb = grid_for(npix, 128, 65535);
 	if (sp.C == 1) gather_pt<1>(gb, st, T, sp, t_lo, f_hi, soff, sl, vals, acc, wacc);

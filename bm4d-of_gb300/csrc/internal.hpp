@@ -101,15 +101,23 @@ cudaError_t launch_paste_resolve(const Tile *tiles, int ntiles, const int *grid,
 cudaError_t launch_count_alive(const Tile *tiles, int ntiles, long long G, const uint8_t *alive,
                                unsigned *counts, cudaStream_t st);
 cudaError_t exclusive_scan(unsigned *data, size_t n, unsigned *scratch, cudaStream_t st);
+unsigned scan_kernels(size_t n);
+// launch_lists and launch_gather add the kernels they launch to *launches
 cudaError_t launch_lists(long long ga, long long gb, int np, const uint8_t *nsimp,
                          const uint32_t *idx, const uint8_t *alive, size_t npos, unsigned *cnt,
-                         unsigned *off, unsigned *list, unsigned *scratch, cudaStream_t st);
-// Ordered gather of the slots whose origins lie in frames [t_lo, t_hi]:
-// spatial lists (soff: npos+1 entries, sl: px*px entries per slot), then the
-// per-pixel merge over origin frames.
+                         unsigned *off, unsigned *list, unsigned *scratch, unsigned *launches, cudaStream_t st);
+// Ordered gather of the slots whose origins lie in frames [t_lo, t_hi].  4x4
+// patches (quad_path): row lists (offsets in cnt) and quad lists (offsets in
+// soff), both in sl, then a merge over origin frames per quad of 4 pixels;
+// other patches: spatial lists (soff), then a merge per pixel.  cnt and soff
+// hold npos+1 entries, sl list_entries_per_member(sp) entries per slot of a
+// chunk of `members` slots.
+bool quad_path(const StepParams &sp);
+int list_entries_per_member(const StepParams &sp);
 cudaError_t launch_gather(const Tile &T, const StepParams &sp, int t_lo, int t_hi,
-                          const unsigned *off, const unsigned *list, unsigned *soff, unsigned *sl,
-                          unsigned *scratch, const float *vals, float *acc, float *wacc, cudaStream_t st);
+                          const unsigned *off, const unsigned *list, unsigned *cnt, unsigned *soff, unsigned *sl,
+                          size_t members, unsigned *scratch, const float *vals, float *acc, float *wacc,
+                          unsigned *launches, cudaStream_t st);
 cudaError_t launch_color(const Image &in, const Image &out, int forward, cudaStream_t st);
 cudaError_t launch_finalize(const Tile *tiles, int nW, int wTmp, int hTmp, const StepParams &sp,
                             const Image &noisy, const float *acc, const float *wacc,

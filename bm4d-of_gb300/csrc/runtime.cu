@@ -565,7 +565,8 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	DBUF("off", pl.maxpos + 1, S.d_off);
 	DBUF("soff", pl.maxpos + 1, S.d_soff);
 	DBUF("scratch", pl.maxpos / 4096 + pl.maxpos / (4096ull * 4096ull) + 64, S.d_scratch);
-	const size_t per_group = (size_t)sp.np * ((size_t)term_stride(C) * sp.spc + 1 + (size_t)sp.px * sp.px) * sizeof(float) +
+	const size_t per_group = (size_t)sp.np * ((size_t)term_stride(C) * sp.spc + 1 + (size_t)list_entries_per_member(sp)) *
+	                             sizeof(float) +
 	                         (mode.learned ? (size_t)kMlpInPad * 2 + (size_t)kMlpOutN * 4 : 0);
 	size_t budget = ctx->slot_budget;
 	long long chunk = std::max<long long>(1, (long long)(budget / per_group));
@@ -575,7 +576,7 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	if (!mode.samples) {
 		DBUF("vals", (size_t)chunk * sp.np * term_stride(C) * sp.spc, S.d_vals);
 		DBUF("list", (size_t)chunk * sp.np, S.d_list);
-		DBUF("slist", (size_t)chunk * sp.np * sp.px * sp.px, S.d_sl);
+		DBUF("slist", (size_t)chunk * sp.np * list_entries_per_member(sp), S.d_sl);
 	}
 	if (mode.learned) {
 		DBUF("lfeat", (size_t)chunk * kMlpInPad, S.d_lfeat);
@@ -732,8 +733,7 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 			{
 				Mark m(ctx, T_AGG);
 				CK(launch_lists(ga, gb, sp.np, S.d_nsimp, S.d_idx, S.d_alive, npos, S.d_cnt, S.d_off, S.d_list,
-				                S.d_scratch, st));
-				ctx->launches += 5;
+				                S.d_scratch, &ctx->launches, st));
 				// origin frames of the chunk's member patches: the temporal search
 				// range of a reference frame t lies within t -/+ (wtb + wtf)
 				const long long fa = (ga - T.g0) / ((long long)T.nx * T.ny);
@@ -742,9 +742,9 @@ bm4dof_status launch_step(bm4dof_ctx *ctx, int slot, const Image &noisy, const I
 				const int reach = sp.wtb + sp.wtf;
 				const int t_lo = std::max(0, ta - reach);
 				const int t_hi = std::min((int)F - sp.pt, tb + reach);
-				CK(launch_gather(T, sp, t_lo, t_hi, S.d_off, S.d_list, S.d_soff, S.d_sl, S.d_scratch, S.d_vals,
-				                 S.d_acc + T.pix0 * C, S.d_wacc + T.pix0, st));
-				ctx->launches += 4;
+				CK(launch_gather(T, sp, t_lo, t_hi, S.d_off, S.d_list, S.d_cnt, S.d_soff, S.d_sl,
+				                 (size_t)chunk * sp.np, S.d_scratch, S.d_vals, S.d_acc + T.pix0 * C,
+				                 S.d_wacc + T.pix0, &ctx->launches, st));
 			}
 		}
 	}

@@ -28,11 +28,18 @@ def term_stride(C):
     return 2 if C == 1 else (4 if C <= 3 else 8)
 
 
+def list_entries(p):
+    """List entries per member: 4x4 patches take the quad path (at most 2 row-
+    list and 8 quad-list entries), other sizes px*px spatial-list entries."""
+    quad = p.sizePatch == 4 and p.sizePatchTime in (1, 2, 4)
+    return 10 if quad else p.sizePatch * p.sizePatch
+
+
 def chunk_bytes(p, C):
     """Bytes one group takes in a chunk (the runtime's per-group budget):
-    np x (terms of every patch element, origin list entry, spatial lists)."""
+    np x (terms of every patch element, origin list entry, gather lists)."""
     spc = p.sizePatch * p.sizePatch * p.sizePatchTime
-    return p.nSimilarPatches * (term_stride(C) * spc + 1 + p.sizePatch * p.sizePatch) * 4
+    return p.nSimilarPatches * (term_stride(C) * spc + 1 + list_entries(p)) * 4
 
 
 def gparams(gpulib, arr):
@@ -69,8 +76,8 @@ def test_gpu_golden_in_small_chunks(gpulib, gpuctx, case, monkeypatch):
     basic, final, ratios = gpuctx.runNlBayes(g["noisy"], g.get("fflow"), g.get("bflow"), p1, p2, nparts=nparts)
     launches = gpuctx.timings()[1]
     monkeypatch.delenv("BM4DOF_SLOT_MB")
-    # 11 launches per chunk (filter 2, origin lists 5, gather 4)
-    assert launches >= one_chunk_launches + 11 * extra, (launches, one_chunk_launches, extra)
+    # at least 10 launches per chunk (filter 2, origin lists 4, gather 4 or more)
+    assert launches >= one_chunk_launches + 10 * extra, (launches, one_chunk_launches, extra)
     assert np.array_equal(basic, g["basic"], equal_nan=True)
     assert np.array_equal(final, g["final"], equal_nan=True)
     assert ratios == tuple(g["ratios"].tolist())
