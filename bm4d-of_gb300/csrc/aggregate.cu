@@ -672,8 +672,9 @@ __global__ void qlist_build_kernel(int h, int nq, int nf, const unsigned *__rest
 // slot order, the order of the reference's scatter loop for every pixel.  A
 // member adds to the pixels j of the quad with 0 <= j - s < 4 (s = ox - 4q),
 // from element dx = j - s of its row.  Members are fetched D ahead of the one
-// being added (a register ring consumed in fetch order), so that up to 4*D
-// term loads of a thread are in flight.
+// being added (a register ring consumed in fetch order).  One member ahead
+// measured best on 1920x1080x60 (aggregation 434 ms per step against 446 ms
+// with two and 533 ms with four): fewer registers, more resident warps.
 template <int PT, int CC>
 __global__ void __launch_bounds__(128)
 gather_quad_kernel(Tile T, StepParams sp, int t_lo, int t_hi, int f_hi, int nq, const unsigned *__restrict__ qoff,
@@ -681,7 +682,7 @@ gather_quad_kernel(Tile T, StepParams sp, int t_lo, int t_hi, int f_hi, int nq, 
                    float *__restrict__ wacc)
 {
 	constexpr int TS = CC == 1 ? 2 : (CC <= 3 ? 4 : 8);
-	constexpr int D = CC == 1 ? 4 : 2;
+	constexpr int D = 1;
 	const int w = T.w, h = T.h, spc = sp.spc;
 	const size_t wh = (size_t)w * h, plane = (size_t)nq * h;
 	const size_t n = plane * (size_t)(f_hi - t_lo + 1);

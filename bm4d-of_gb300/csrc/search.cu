@@ -17,8 +17,8 @@
 //                  every frame of its temporal range (a short dependent chain
 //                  of flow reads, kept out of the distance kernel);
 //   search_kernel  one CTA per group at a time: warp 0 lays out the candidate
-//                  windows; every thread computes column strips of kR
-//                  vertically adjacent candidates (lanes on consecutive
+//                  windows; every thread computes column strips of R (21 or
+//                  7) vertically adjacent candidates (lanes on consecutive
 //                  columns, window rows read through L1, the reference patch
 //                  from shared memory one patch frame at a time into
 //                  registers); the distances land in shared memory in the
@@ -39,7 +39,7 @@ namespace bm4dof {
 
 namespace {
 
-constexpr int kThreads = 192;          // 6 warps: 567 column strips of a 21x21x9 window set in 3 rounds
+constexpr int kThreads = 192;          // 6 warps: the 189 window columns of a 21x21x9 window set in one round
 
 struct FrameWin {
 	int qt, rx0, ry0, nx, ny, cbase, ibase;
@@ -95,7 +95,7 @@ struct SearchArgs {
 
 // Window table of one group, one lane per frame of the temporal range
 // (warp 0): candidate and column-strip offsets by warp prefix sums.
-__device__ void plan_group(const SearchArgs &a, const StepParams &sp, long long g, FrameWin *fw, int &nframes,
+__device__ void plan_group(const SearchArgs &a, const StepParams &sp, long long g, int R, FrameWin *fw, int &nframes,
                            int &ncand, int &nitems, int &tile, int &gx, int &gy, int &gt)
 {
 	const int lane = threadIdx.x & 31;
@@ -121,7 +121,7 @@ __device__ void plan_group(const SearchArgs &a, const StepParams &sp, long long 
 		f.nx = max(0, rx1 - rx0 + 1);
 		f.ny = max(0, ry1 - ry0 + 1);
 		cnt = f.nx * f.ny;
-		items = f.nx * ((f.ny + kR - 1) / kR);
+		items = f.nx * ((f.ny + R - 1) / R);
 	}
 	int ic = cnt, ii = items;
 #pragma unroll
@@ -276,10 +276,10 @@ __device__ void select_knn(const float *dist, int ncand, int K, float tmin, Sele
 }
 
 // One CTA handles one group at a time: every thread computes column strips of
-// kR candidates (window rows read through L1 from the video), then the CTA
+// R candidates (window rows read through L1 from the video), then the CTA
 // selects the k nearest.  Several CTAs share an SM so that one CTA's
 // selection overlaps the others' distance work.
-template <int PX, int PT, bool REFREG, int MINB>
+template <int PX, int PT, bool REFREG, int MINB, int R>
 __global__ void __launch_bounds__(kThreads, MINB)
 search_kernel(Image src, StepParams sp, SearchArgs a)
 {
@@ -295,7 +295,7 @@ search_kernel(Image src, StepParams sp, SearchArgs a)
 	const long long ng = a.glist ? (long long)*a.gcount : a.g_end - a.g_begin;
 	for (long long gi = blockIdx.x; gi < ng; gi += gridDim.x) {
 		const long long g = a.glist ? (long long)a.glist[gi] : a.g_begin + gi;
-		if (tid < 32) plan_group(a, sp, g, fw, s_nframes, s_ncand, s_nitems, s_tile, s_x, s_y, s_t);
+		if (tid < 32) plan_group(a, sp, g, R, fw, s_nframes, s_ncand, s_nitems, s_tile, s_x, s_y, s_t);
 		__syncthreads();
 		const Tile T = a.tiles[s_tile];
 		const int nframes = s_nframes;
@@ -324,14 +324,14 @@ search_kernel(Image src, StepParams sp, SearchArgs a)
 			const FrameWin f = fw[ii];
 			const int rel = it - f.ibase;
 			const int rb = rel / f.nx, cx = rel - rb * f.nx;   // row block, column
-			const int qy0 = rb * kR;
-			float acc[kR];
+			const int qy0 = rb * R;
+			float acc[R];
 			const float *colp = src.p + src.at(T.ox + f.rx0 + cx, T.oy + f.ry0 + qy0, f.qt, 0);
-			col_distances<PX, PT, REFREG>(colp, src.P, src.plane(), src.plane() * src.C, f.ny - qy0 + sp.px - 2,
+			col_distances<PX, PT, REFREG, R>(colp, src.P, src.plane(), src.plane() * src.C, f.ny - qy0 + sp.px - 2,
 			                              chn, sp.px, sp.pt, ref_s, ref_r, acc);
 			float *dd = dist + f.cbase + qy0 * f.nx + cx;
 #pragma unroll
-			for (int r = 0; r < kR; r++)
+			for (int r = 0; r < R; r++)
 				if (qy0 + r < f.ny) { dd[r * f.nx] = acc[r]; tmin = fminf(tmin, acc[r]); }
 		}
 		__syncthreads();
@@ -370,11 +370,11 @@ __global__ void search_single_kernel(const Tile *__restrict__ tiles, int ntiles,
 	}
 }
 
-template <int PX, int PT, bool REFREG, int MINB = 1>
+template <int PX, int PT, bool REFREG, int MINB = 1, int R = kR>
 cudaError_t launch_t(const Image &src, const StepParams &sp, const SearchArgs &a, size_t smem, int nsm,
                      long long n, cudaStream_t st)
 {
-	auto kern = search_kernel<PX, PT, REFREG, MINB>;
+	auto kern = search_kernel<PX, PT, REFREG, MINB, R>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
 	int per_sm = 0;
@@ -441,6 +441,11 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
 		// four (80 registers) and five (64): 133 vs 137 vs 147 ms on 854x480x20
 		if (one) return launch_t<4, 4, true>(src, sp, a, smem, nsm, n, st);
 		if (sp.search_ctas == 4) return launch_t<4, 4, false, 4>(src, sp, a, smem, nsm, n, st);
+		// whole 21-row window columns per thread (24 rows loaded for 21
+		// candidates instead of 30 for three strips of 7): 124.9 -> 112.0 ms on
+		// 854x480x20, 2146 -> 1947 ms on 1920x1080x60; windows under 15 rows
+		// keep strips of 7
+		if (sp.wx >= 15) return launch_t<4, 4, false, 6, 21>(src, sp, a, smem, nsm, n, st);
 		return launch_t<4, 4, false, 6>(src, sp, a, smem, nsm, n, st);
 	}
 	if (sp.px == 8 && sp.pt == 1)

@@ -111,19 +111,20 @@ __device__ __forceinline__ int visit_frame(int ii, int t, int t1)
 	return ii == 0 ? t : (ii <= t1 - t ? t + ii : t - (ii - (t1 - t)));
 }
 
-// Distances of kR vertically adjacent candidates (one column of the window,
-// rows r = 0..kR-1 below `col`, which points at candidate row 0, patch frame
+// Distances of R vertically adjacent candidates (one column of the window,
+// rows r = 0..R-1 below `col`, which points at candidate row 0, patch frame
 // 0, channel 0).  Each image row is loaded once and feeds every candidate
 // whose patch covers it; per candidate the terms still follow the reference's
 // (c, ht, hy, hx) order.  Consecutive lanes take consecutive columns, so each
 // warp-wide load touches one or two contiguous row segments.  With the
 // reference patch in shared memory (ref_s, 16-byte aligned), small patches
 // take one patch frame of it at a time into registers with vector loads.
-template <int PX, int PT, bool REFREG>
+template <int PX, int PT, bool REFREG, int R>
 __device__ __forceinline__ void col_distances(const float *col, size_t rpitch, size_t cpitch, size_t tpitch,
                                               int ymax, int chn, int px_rt, int pt_rt, const float *ref_s,
-                                              const float (&ref_r)[(PX > 0 ? PX * PX * PT : 1)], float acc[kR])
+                                              const float (&ref_r)[(PX > 0 ? PX * PX * PT : 1)], float (&acc)[R])
 {
+	constexpr int kR = R;   // candidates of the strip
 #pragma unroll
 	for (int r = 0; r < kR; r++) acc[r] = 0.f;
 	if (PX > 0) {
