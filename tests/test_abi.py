@@ -28,6 +28,16 @@ def test_version_and_error_without_device(gpulib):
     assert lib.bm4dof_last_error() is not None
 
 
+def test_stream_getters_refuse_null_handles(gpulib):
+    """bm4dof_get_stream / bm4dof_trainer_get_stream check their arguments
+    before touching a device."""
+    lib = gpulib.load()
+    out = ctypes.c_void_p()
+    assert lib.bm4dof_get_stream(None, ctypes.byref(out)) == 1
+    assert lib.bm4dof_trainer_get_stream(None, ctypes.byref(out)) == 1
+    assert b"null" in lib.bm4dof_last_error()
+
+
 def test_no_cpu_fallback_when_library_missing(tmp_path):
     import importlib
     import bm4dof
