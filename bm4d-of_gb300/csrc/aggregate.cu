@@ -444,7 +444,9 @@ gather_slist_kernel(Tile T, StepParams sp, int f_lo, int f_hi, const unsigned *_
                     const unsigned *__restrict__ sl, const float *__restrict__ vals, float *__restrict__ acc,
                     float *__restrict__ wacc)
 {
-	constexpr int L = PT > 0 ? PT : kMaxSpc;
+	// any other pt: up to kMaxGatherPt lists (a 64-element patch of px >= 2 has
+	// at most 16 frames; runs with more patch frames are refused)
+	constexpr int L = PT > 0 ? PT : kMaxGatherPt;
 	const int px = sp.px, pt = PT > 0 ? PT : sp.pt, spc = sp.spc;
 	const size_t wh = (size_t)T.w * T.h;
 	const size_t n = wh * (size_t)(f_hi - f_lo + 1);

@@ -18,6 +18,7 @@ namespace bm4dof {
 
 constexpr int kMaxNp = 32;        // largest number of similar patches kept
 constexpr int kMaxSpc = 64;       // largest patch size px*px*pt on the fast paths
+constexpr int kMaxGatherPt = 16;  // largest sizePatchTime (a 64-element patch of px >= 2)
 constexpr int kMaxFrames = 32;    // largest temporal search range (wtb+wtf+1)
 
 struct Image {                    // one full-frame planar video on the device

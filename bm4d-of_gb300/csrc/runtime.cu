@@ -304,6 +304,7 @@ bm4dof_status check_params(const bm4dof_params &p)
 	else if (p.offSet == 0 || p.offSetTime == 0) why = "offSet and offSetTime must be positive";
 	else if (p.nSimilarPatches == 0 || p.nSimilarPatches > (unsigned)kMaxNp) why = "nSimilarPatches must be in [1, 32]";
 	else if (spc > (unsigned)kMaxSpc) why = "sizePatch^2 * sizePatchTime must be at most 64";
+	else if (p.sizePatchTime > (unsigned)kMaxGatherPt) why = "sizePatchTime must be at most 16";
 	else if (p.sizeSearchWindow == 0) why = "sizeSearchWindow must be positive";
 	else if (p.sizeSearchTimeRangeFwd + p.sizeSearchTimeRangeBwd + 1 > (unsigned)kMaxFrames) why = "temporal search range too long";
 	else if (p.sigma <= 0.f) why = "sigma must be positive";

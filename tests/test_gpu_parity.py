@@ -164,6 +164,11 @@ def test_gpu_errors(gpulib, gpuctx):
     with pytest.raises(gpulib.BM4DOFError) as e:
         gpuctx.runNlBayes(nz, None, None, *q)
     assert e.value.status == "ERR_UNSUPPORTED"
+    q = resolve_params(gpulib, (W, H, F, 1), 20.0, **CFG_VIDEO)
+    q[1].sizePatch, q[1].sizePatchTime = 1, 17   # 17 values, but more patch frames than the gather takes
+    with pytest.raises(gpulib.BM4DOFError) as e:
+        gpuctx.runNlBayes(nz, None, None, *q)
+    assert e.value.status == "ERR_UNSUPPORTED" and "sizePatchTime" in str(e.value)
     # the context stays usable after errors
     clean, nz, ff, bf = video_case(W + 8, H + 8, F + 3, seed=3)
     p = resolve_params(gpulib, (W + 8, H + 8, F + 3, 1), 20.0, **CFG_VIDEO)
