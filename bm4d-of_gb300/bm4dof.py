@@ -113,7 +113,8 @@ class Sequence(C.Structure):
 
 class Tuning(C.Structure):
     """bm4dof_tuning: launch shape of a batched run."""
-    _fields_ = [("branches", C.c_uint), ("slot_mb", C.c_uint), ("search_ctas", C.c_uint)]
+    _fields_ = [("branches", C.c_uint), ("slot_mb", C.c_uint), ("search_ctas", C.c_uint),
+                ("search_strip", C.c_uint), ("gather_depth", C.c_uint)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -460,16 +461,17 @@ class Context:
         return [(q.ratios[0], q.ratios[1]) for q in arr]
 
     def autotune(self, items, sample=16, mixed=False, learned=False, vbm3d=False):
-        """(best tuning dict, table of (branches, slot_mb, search_ctas, ms))."""
+        """(best tuning dict, table of (branches, slot_mb, search_ctas, search_strip,
+        gather_depth, ms))."""
         arr = self._sequences(items)
         flags = _mixed_flags(mixed) | (LEARNED if learned else 0) | (VBM3D_SEARCH if vbm3d else 0)
         best = Tuning()
-        table = (C.c_float * (4 * 32))()
+        table = (C.c_float * (6 * 32))()
         rows = C.c_uint()
         with self._ordered():
             _check(load().bm4dof_autotune(self._h, arr, len(items), sample, flags, C.byref(best), table, 32,
                                           C.byref(rows)))
-        tab = [tuple(table[4 * i:4 * i + 4]) for i in range(min(rows.value, 32))]
+        tab = [tuple(table[6 * i:6 * i + 6]) for i in range(min(rows.value, 32))]
         return best.as_dict(), tab
 
     def set_gain_network(self, params=None, kappa=0.0):

@@ -676,15 +676,15 @@ __global__ void qlist_build_kernel(int h, int nq, int nf, const unsigned *__rest
 // from element dx = j - s of its row.  Members are fetched D ahead of the one
 // being added (a register ring consumed in fetch order).  One member ahead
 // measured best on 1920x1080x60 (aggregation 434 ms per step against 446 ms
-// with two and 533 ms with four): fewer registers, more resident warps.
-template <int PT, int CC>
+// with two and 533 ms with four): fewer registers, more resident warps; the
+// batched runs' tuning may choose two (gather_depth).
+template <int PT, int CC, int D>
 __global__ void __launch_bounds__(128)
 gather_quad_kernel(Tile T, StepParams sp, int t_lo, int t_hi, int f_hi, int nq, const unsigned *__restrict__ qoff,
                    const unsigned *__restrict__ ql, const float *__restrict__ vals, float *__restrict__ acc,
                    float *__restrict__ wacc)
 {
 	constexpr int TS = CC == 1 ? 2 : (CC <= 3 ? 4 : 8);
-	constexpr int D = 1;
 	const int w = T.w, h = T.h, spc = sp.spc;
 	const size_t wh = (size_t)w * h, plane = (size_t)nq * h;
 	const size_t n = plane * (size_t)(f_hi - t_lo + 1);
@@ -794,21 +794,29 @@ gather_quad_kernel(Tile T, StepParams sp, int t_lo, int t_hi, int f_hi, int nq, 
 	}
 }
 
+template <int CC, int D>
+void gather_quad_d(int gb, cudaStream_t st, const Tile &T, const StepParams &sp, int t_lo, int t_hi, int f_hi,
+                   int nq, const unsigned *qoff, const unsigned *ql, const float *vals, float *acc, float *wacc)
+{
+	switch (sp.pt) {
+	case 1:
+		gather_quad_kernel<1, CC, D><<<gb, 128, 0, st>>>(T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
+		break;
+	case 2:
+		gather_quad_kernel<2, CC, D><<<gb, 128, 0, st>>>(T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
+		break;
+	default:
+		gather_quad_kernel<4, CC, D><<<gb, 128, 0, st>>>(T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
+		break;
+	}
+}
+
 template <int CC>
 void gather_quad_pt(int gb, cudaStream_t st, const Tile &T, const StepParams &sp, int t_lo, int t_hi, int f_hi,
                     int nq, const unsigned *qoff, const unsigned *ql, const float *vals, float *acc, float *wacc)
 {
-	switch (sp.pt) {
-	case 1:
-		gather_quad_kernel<1, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
-		break;
-	case 2:
-		gather_quad_kernel<2, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
-		break;
-	default:
-		gather_quad_kernel<4, CC><<<gb, 128, 0, st>>>(T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
-		break;
-	}
+	if (sp.gather_depth == 2) gather_quad_d<CC, 2>(gb, st, T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
+	else gather_quad_d<CC, 1>(gb, st, T, sp, t_lo, t_hi, f_hi, nq, qoff, ql, vals, acc, wacc);
 }
 
 template <int CC>

@@ -51,6 +51,8 @@ struct StepParams {               // resolved parameters of one step
 	int use_flow;
 	float beta1;                  // learned form: hard threshold of the non-mean Haar rows
 	int search_ctas;              // exact search: CTAs per SM (4 or 6; 0 = default)
+	int search_strip;             // exact search: candidates per thread along a column (7 or 21; 0 = default)
+	int gather_depth;             // quad gather: members in flight per thread (1 or 2; 0 = 1)
 	float beta_mean;              // betaMean (order-invariant filtering)
 	int order_inv;                // orderInvariance
 	int vbm3d;                    // predictive search (the reference's VBM3D_SEARCH build)

@@ -65,6 +65,8 @@ struct bm4dof_ctx {
 	bool fixed_budget = false;   // batched children: slot_budget set by the tuning
 	bool no_marks = false;       // inside a graph capture: no timing events
 	int search_ctas = 0;         // exact search CTAs per SM (0: default)
+	int search_strip = 0;        // exact search candidates per thread along a column (0: default)
+	int gather_depth = 0;        // quad gather members in flight per thread (0: 1)
 	size_t held = 0;          // device bytes held in bufs
 	size_t mem_limit = 0;     // cap on held (0: none), bm4dof_set_memory_limit
 	std::recursive_mutex mu;  // calls on one context are serialised (CtxLock)
@@ -471,6 +473,8 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	sp.use_flow = use_flow ? 1 : 0;
 	sp.beta1 = mode.beta1;
 	sp.search_ctas = ctx->search_ctas;
+	sp.search_strip = ctx->search_strip;
+	sp.gather_depth = ctx->gather_depth;
 	sp.beta_mean = p.betaMean;
 	sp.order_inv = p.orderInvariance ? 1 : 0;
 	sp.vbm3d = mode.vbm3d ? 1 : 0;
@@ -1362,6 +1366,8 @@ bm4dof_status run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n, un
 			c->st = X.branches[i % nb];
 			c->slot_budget = per_child;
 			c->search_ctas = tu.search_ctas;
+			c->search_strip = tu.search_strip;
+			c->gather_depth = tu.gather_depth;
 			c->kappa = ctx->kappa;
 			c->has_gain = ctx->has_gain;
 			c->whf = (float)(args[i].W * args[i].H * args[i].F);
@@ -1467,9 +1473,17 @@ bm4dof_status bm4dof_run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigne
 		set_error("bm4dof_run_batched: unsupported flags");
 		return BM4DOF_ERR_UNSUPPORTED;
 	}
-	bm4dof_tuning t = tuning ? *tuning : bm4dof_tuning{0, 0, 0};
+	bm4dof_tuning t = tuning ? *tuning : bm4dof_tuning{0, 0, 0, 0, 0};
 	if (t.search_ctas != 0 && t.search_ctas != 4 && t.search_ctas != 6) {
 		set_error("bm4dof_run_batched: search_ctas must be 0, 4 or 6");
+		return BM4DOF_ERR_ARGUMENT;
+	}
+	if (t.search_strip != 0 && t.search_strip != 7 && t.search_strip != 21) {
+		set_error("bm4dof_run_batched: search_strip must be 0, 7 or 21");
+		return BM4DOF_ERR_ARGUMENT;
+	}
+	if (t.gather_depth > 2) {
+		set_error("bm4dof_run_batched: gather_depth must be 0, 1 or 2");
 		return BM4DOF_ERR_ARGUMENT;
 	}
 	return run_batched(ctx, seqs, n, flags, t);
@@ -1496,16 +1510,18 @@ bm4dof_status bm4dof_autotune(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n
 		}
 		ms *= 0.5f;
 		if (table && nrow < cap) {
-			float *row = table + 4 * nrow;
+			float *row = table + 6 * nrow;
 			row[0] = (float)t.branches;
 			row[1] = (float)t.slot_mb;
 			row[2] = (float)t.search_ctas;
-			row[3] = ms;
+			row[3] = (float)t.search_strip;
+			row[4] = (float)t.gather_depth;
+			row[5] = ms;
 		}
 		nrow++;
 		return BM4DOF_OK;
 	};
-	bm4dof_tuning cur = {std::min(m, 16u), 1024, 6};
+	bm4dof_tuning cur = {std::min(m, 16u), 1024, 6, 21, 1};
 	float best_ms = 0.f;
 	bm4dof_status e = time_one(cur, best_ms);
 	if (e != BM4DOF_OK) return e;
@@ -1528,8 +1544,23 @@ bm4dof_status bm4dof_autotune(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n
 		if (ms < best_ms) { best_ms = ms; cur = t; }
 	}
 	{
+		// the exact search's tile shape: 21 or 7 candidates per thread along a
+		// window column at 6 CTAs per SM, or strips of 7 at 4 CTAs per SM
+		const bm4dof_tuning b2 = cur;
+		const unsigned shapes[2][2] = {{6, 7}, {4, 7}};
+		for (const auto &sh : shapes) {
+			bm4dof_tuning t = b2;
+			t.search_ctas = sh[0];
+			t.search_strip = sh[1];
+			float ms;
+			if ((e = time_one(t, ms)) != BM4DOF_OK) return e;
+			if (ms < best_ms) { best_ms = ms; cur = t; }
+		}
+	}
+	{
+		// the gather's staging depth: members in flight per thread
 		bm4dof_tuning t = cur;
-		t.search_ctas = 4;
+		t.gather_depth = 2;
 		float ms;
 		if ((e = time_one(t, ms)) != BM4DOF_OK) return e;
 		if (ms < best_ms) { best_ms = ms; cur = t; }

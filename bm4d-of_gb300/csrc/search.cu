@@ -444,8 +444,9 @@ cudaError_t launch_search(const Image &src, const Tile *tiles, int ntiles, const
 		// whole 21-row window columns per thread (24 rows loaded for 21
 		// candidates instead of 30 for three strips of 7): 124.9 -> 112.0 ms on
 		// 854x480x20, 2146 -> 1947 ms on 1920x1080x60; windows under 15 rows
-		// keep strips of 7
-		if (sp.wx >= 15) return launch_t<4, 4, false, 6, 21>(src, sp, a, smem, nsm, n, st);
+		// keep strips of 7 (search_strip: the batched runs' tuning)
+		if (sp.search_strip == 21 || (sp.search_strip == 0 && sp.wx >= 15))
+			return launch_t<4, 4, false, 6, 21>(src, sp, a, smem, nsm, n, st);
 		return launch_t<4, 4, false, 6>(src, sp, a, smem, nsm, n, st);
 	}
 	if (sp.px == 8 && sp.pt == 1)

@@ -289,6 +289,11 @@ typedef struct bm4dof_tuning {
 	unsigned slot_mb;      /* per sequence: MB of aggregation terms per chunk
 	                          (the depth of group staging); 0: 1024              */
 	unsigned search_ctas;  /* exact search CTAs per SM: 4 or 6; 0: 6             */
+	unsigned search_strip; /* exact search candidates per thread along a window
+	                          column: 7 or 21; 0: 21 for windows of 15 rows or
+	                          more (4x4x4 patches, 6 CTAs per SM)                */
+	unsigned gather_depth; /* members in flight per thread of the ordered
+	                          gather (4x4 patches): 1 or 2; 0: 1                */
 } bm4dof_tuning;
 
 /* Denoises n sequences (flags: BM4DOF_MIXED_PRECISION, BM4DOF_LEARNED,
@@ -300,9 +305,10 @@ bm4dof_status bm4dof_run_batched(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigne
                                  const bm4dof_tuning *tuning);
 
 /* Times candidate tunings (graph replays of the first `sample` sequences,
- * coordinate descent over branches, slot_mb and search_ctas) and returns the
- * fastest in *best.  table (may be NULL) receives up to cap rows of
- * {branches, slot_mb, search_ctas, milliseconds} as floats; *rows = count. */
+ * coordinate descent over branches, slot_mb, search_ctas, search_strip and
+ * gather_depth) and returns the fastest in *best.  table (may be NULL)
+ * receives up to cap rows of {branches, slot_mb, search_ctas, search_strip,
+ * gather_depth, milliseconds} as floats; *rows = count. */
 bm4dof_status bm4dof_autotune(bm4dof_ctx *ctx, bm4dof_sequence *seqs, unsigned n, unsigned sample,
                               unsigned flags, bm4dof_tuning *best, float *table, unsigned cap, unsigned *rows);
 

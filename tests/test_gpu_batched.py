@@ -51,10 +51,20 @@ def test_batched_replay_and_autotune(gpulib, gpuctx):
         assert bool((a == it["final"]).all())
     best, table = gpuctx.autotune(items, sample=4)
     assert best["branches"] >= 1 and best["slot_mb"] in (256, 1024, 4096) and best["search_ctas"] in (4, 6)
-    assert len(table) >= 4 and all(row[3] > 0 for row in table)
+    assert best["search_strip"] in (7, 21) and best["gather_depth"] in (1, 2)
+    assert len(table) >= 6 and all(row[5] > 0 for row in table)
+    # every tile shape and staging depth was timed
+    assert {(r[2], r[3]) for r in table} >= {(6, 21), (6, 7), (4, 7)} and {r[4] for r in table} == {1, 2}
     gpuctx.run_batched(items, tuning=best)
     for a, it in zip(first, items):
         assert bool((a == it["final"]).all())
+    # the other shapes and depths give the same outputs
+    for tu in ({"search_strip": 7}, {"gather_depth": 2}, {"search_ctas": 4, "search_strip": 7}):
+        gpuctx.run_batched(items, tuning=dict(best, **tu))
+        for a, it in zip(first, items):
+            assert bool((a == it["final"]).all()), tu
+    with pytest.raises(gpulib.BM4DOFError):
+        gpuctx.run_batched(items, tuning=dict(best, search_strip=9))
 
 
 def test_batched_learned_matches_unbatched(gpulib, gpuctx):
