@@ -566,7 +566,7 @@ bm4dof_status prepare_step(bm4dof_ctx *ctx, int slot, int step, const bm4dof_par
 	// numbers must fit 26 bits
 	DBUF("acc", pl.pix * C, S.d_acc);
 	DBUF("wacc", pl.pix, S.d_wacc);
-	DBUF("cnt", pl.maxpos, S.d_cnt);
+	DBUF("cnt", pl.maxpos + 1, S.d_cnt);   // also the quad path's row-list offsets: ceil(w/4)*h*F + 1 entries
 	DBUF("off", pl.maxpos + 1, S.d_off);
 	DBUF("soff", pl.maxpos + 1, S.d_soff);
 	DBUF("scratch", pl.maxpos / 4096 + pl.maxpos / (4096ull * 4096ull) + 64, S.d_scratch);
