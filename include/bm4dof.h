@@ -291,7 +291,8 @@ typedef struct bm4dof_tuning {
 	unsigned search_ctas;  /* exact search CTAs per SM: 4 or 6; 0: 6             */
 	unsigned search_strip; /* exact search candidates per thread along a window
 	                          column: 7 or 21; 0: 21 for windows of 15 rows or
-	                          more (4x4x4 patches, 6 CTAs per SM)                */
+	                          more (4x4x4 patches at 6 CTAs per SM; at 4 CTAs
+	                          per SM and for other patches the strip is 7)      */
 	unsigned gather_depth; /* members in flight per thread of the ordered
 	                          gather (4x4 patches): 1 or 2; 0: 1                */
 } bm4dof_tuning;
