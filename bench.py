@@ -48,7 +48,9 @@ WORKLOADS = {
 CLI = dict(px1=4, px2=4, pt1=4, pt2=4, wx1=21, wx2=21, np1=16, np2=16, b1=3.0)
 METRIC = "megapixel-frames/s at 1 GPU, plain vs learned/mixed at ≤0.05 dB PSNR loss"
 UNIT = "MPF/s"
-SEARCH_TRAFFIC_SMALL = 11.24e6 + 0.648e6
+# ncu dram__bytes_read + dram__bytes_write of one step-1 search_kernel launch on
+# 480x272x12 (one --set full capture of the small workload)
+SEARCH_TRAFFIC_SMALL = 12.04e6 + 7.60e6
 # CPU sample (crop of the same workload) for the host-core baseline: 12
 # frames, so that every reference patch has the full 9-frame search range it
 # has in the long video
@@ -461,7 +463,7 @@ def main():
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
                      # DRAM bytes per launch: ncu capture of the 480x272x12 step-1 launch
-                     # (11.24 MB read + 0.27 MB written), scaled by the pixel count
+                     # (12.04 MB read + 7.60 MB written), scaled by the pixel count
                      "traffic": SEARCH_TRAFFIC_SMALL * (W * H * F) / (480 * 272 * 12),
                      "traffic_source": "ncu dram__bytes_read+write of search_kernel on 480x272x12, "
                                        "scaled by pixels (the frames and flows, read about once)",
