@@ -23,6 +23,9 @@ CASES = [
     ("video_paste_4tiles", 44, 40, 6, 1, 20.0, 24, True, dict(CFG_VIDEO, paste_boost=True), 2),
     ("image_paste", 48, 40, 1, 1, 20.0, 25, False, dict(CFG_IMAGE, paste_boost=True), 1),
     ("rgb_video_paste", 30, 28, 4, 3, 20.0, 26, True, dict(CFG_VIDEO, paste_boost=True), 1),
+    # 3-frame patches: the generic search, filter and per-pixel gather paths
+    ("video_pt3", 36, 32, 6, 1, 20.0, 27, True,
+     dict(px1=4, px2=4, pt1=3, pt2=3, wx1=15, wx2=13, np1=16, np2=16, b1=3.0), 1),
     # the plain two-step method on one 256x256 grey image: 8x8 patches, bior1.5
     # in step 1, Kaiser aggregation window (nldct.cpp:637-714), 2 tiles
     ("config1_image", 256, 256, 1, 1, 20.0, 1, False, CFG_IMAGE, 1),
