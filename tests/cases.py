@@ -23,6 +23,10 @@ CASES = [
     ("video_paste_4tiles", 44, 40, 6, 1, 20.0, 24, True, dict(CFG_VIDEO, paste_boost=True), 2),
     ("image_paste", 48, 40, 1, 1, 20.0, 25, False, dict(CFG_IMAGE, paste_boost=True), 1),
     ("rgb_video_paste", 30, 28, 4, 3, 20.0, 26, True, dict(CFG_VIDEO, paste_boost=True), 1),
+    # 4x4 image patches (one-frame quad gather) and four-channel video
+    ("image_px4", 44, 40, 1, 1, 20.0, 28, False,
+     dict(px1=4, px2=4, pt1=1, pt2=1, wx1=21, wx2=21, np1=16, np2=16, b1=3.0), 1),
+    ("video_c4", 30, 28, 4, 4, 20.0, 29, True, CFG_VIDEO, 1),
     # 3-frame patches: the generic search, filter and per-pixel gather paths
     ("video_pt3", 36, 32, 6, 1, 20.0, 27, True,
      dict(px1=4, px2=4, pt1=3, pt2=3, wx1=15, wx2=13, np1=16, np2=16, b1=3.0), 1),
