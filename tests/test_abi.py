@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import numpy as np
+
 from helpers import ROOT
 
 
@@ -36,6 +38,22 @@ def test_stream_getters_refuse_null_handles(gpulib):
     assert lib.bm4dof_get_stream(None, ctypes.byref(out)) == 1
     assert lib.bm4dof_trainer_get_stream(None, ctypes.byref(out)) == 1
     assert b"null" in lib.bm4dof_last_error()
+
+
+def test_host_outputs_are_written_in_place(gpulib):
+    """runNlBayes on host arrays writes a caller's writable C-contiguous
+    float32 basic/final in place (pinned buffers stay the copy targets) and
+    copies anything else."""
+    shape = (2, 1, 4, 5)
+    a = np.zeros(shape, np.float32)
+    assert gpulib._out_array(a, shape) is a
+    for other in (np.zeros(shape, np.float64), np.zeros((2, 1, 5, 4), np.float32).transpose(0, 1, 3, 2),
+                  np.zeros((2, 20), np.float32)):
+        b = gpulib._out_array(other, shape)
+        assert b is not other and b.dtype == np.float32 and b.shape == shape
+    ro = np.zeros(shape, np.float32)
+    ro.setflags(write=False)
+    assert gpulib._out_array(ro, shape) is not ro
 
 
 def test_no_cpu_fallback_when_library_missing(tmp_path):
